@@ -1,0 +1,294 @@
+#!/usr/bin/env python3
+"""Throughput of the DFSPH step in particle-steps/s on the 1M-fluid dam break.
+
+Workload (one "step" = one frame of mps::System::OnUpdate over the whole scene): 100^3 fluid
+particles (r = 0.005, spacing 0.01, seeded jitter +-0.001) in a 3 x 1.5 x 2 m tank with ~210k
+single-layer wall particles, y up, open top, cubic spline kernel, rho0 1000, viscosity 0.01,
+surface tension 0.05, dt 5e-4, 0.1 % density / divergence tolerances (synthetic data of the
+stated shape; the reference ships no dataset).
+
+value: fluid particles x timed steps / device time (CUDA events on the launching stream, max
+over ranks), inputs resident in HBM.  e2e: the same through the host-buffer C-ABI call
+(mps_step_host: pinned H2D of the state, step, D2H of the state, every step).  roofline: the
+dominant kernel's algorithmic bytes per launch / its mean launch time (CUDA events), against the
+measured HBM copy bandwidth.  cpu_baseline: the FP64 OpenMP oracle on the host cores.
+--impl reference: the reference's own CUDA step (moonsh5009/MPS_CUDA, FP64, rebuilt headless for
+sm_103a) on the same workload; under torchrun only rank 0 runs it.
+With --gpus N > 1 every rank runs its own replica (the step does not shard without a halo
+exchange), so total work grows with N (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s (DFSPH, 1M fluid)"
+UNIT = "particle-steps/s"
+# algorithmic bytes per fluid particle of each kernel (compulsory SoA FP32 traffic) and per
+# boundary particle of a boundary-reading pass
+ALGO_BYTES = {"pressure_A": 44, "pressure_B": 52, "cg_ap": 72}
+BOUNDARY_BYTES = 16
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def radix_passes(sim) -> int:
+    g = sim.grid()
+    cells = g["dims"][0] * g["dims"][1] * g["dims"][2]
+    bits = max(1, math.ceil(math.log2(max(2, cells))))
+    return math.ceil(bits / 8)
+
+
+def cpu_baseline(scene, max_steps: int = 1):
+    """FP64 OpenMP oracle on the host cores: one full step of the same workload."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    o = O.from_scene(scene, threads=threads)
+    t0 = time.perf_counter()
+    o.step(max_steps)
+    dt = time.perf_counter() - t0
+    return {"value": scene.n * max_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{max_steps} full step(s) of {scene.name} ({scene.n} fluid, {scene.nb} boundary) from the "
+                      f"initial state, FP64 OpenMP restatement of the reference step, {dt:.1f} s"}
+
+
+def run_ours(args, scene, rank, world, local_rank):
+    import torch
+    from mps_cuda_gb300 import Simulation, build
+    from mps_cuda_gb300._lib import K_CG_AP, K_PRESSURE_A, K_PRESSURE_B
+
+    build.build()
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    sim = Simulation.from_scene(scene, device=local_rank)
+
+    def barrier():
+        if dist:
+            import torch.distributed as td
+            td.barrier()
+
+    sim.step(args.warmup, stream)
+    torch.cuda.synchronize(dev)
+    st0 = sim.stats()
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        sim.step(args.steps, stream)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize(dev)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    st1 = sim.stats()
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if dist:
+        import torch.distributed as td
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = scene.n * args.steps * world / (ms_max / 1e3)
+    runs = [st1["runs_total"][k] - st0["runs_total"][k] for k in range(3)]
+    iters = [st1["iters_total"][k] - st0["iters_total"][k] for k in range(3)]
+    P = radix_passes(sim)
+    launches = sum(sim.launches_per_step((0, 0, 0), P) for _ in range(args.steps)) + 2 * runs[0] + 3 * runs[1] + 2 * runs[2]
+
+    # ---- e2e through the host-buffer C-ABI call (pinned H2D + step + D2H every step)
+    pin_p = torch.empty((scene.n, 4), dtype=torch.float32, pin_memory=True)
+    pin_v = torch.empty((scene.n, 4), dtype=torch.float32, pin_memory=True)
+    p0, v0 = sim.get_fluid(stream)
+    pin_p.numpy()[:] = p0
+    pin_v.numpy()[:] = v0
+    e2e_steps = max(1, min(args.steps, 10))
+    sim.step_host(pin_p.numpy(), pin_v.numpy(), 1, stream)  # warm
+    torch.cuda.synchronize(dev)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.step_host(pin_p.numpy(), pin_v.numpy(), 1, stream)
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": scene.n * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 32 * scene.n,
+           "d2h_bytes_per_step": 32 * scene.n, "steps": e2e_steps}
+
+    # ---- roofline of the dominant kernel (CUDA events on the same stream, after the timed work)
+    reps = 20
+    t_a = sim.profile_kernel(K_PRESSURE_A, reps, stream)
+    t_b = sim.profile_kernel(K_PRESSURE_B, reps, stream)
+    t_ap = sim.profile_kernel(K_CG_AP, reps, stream)
+    shares = {"pressure_A": t_a * (runs[0] + runs[2]), "pressure_B": t_b * (runs[0] + runs[2]), "cg_ap": t_ap * runs[1]}
+    per = {"pressure_A": t_a, "pressure_B": t_b, "cg_ap": t_ap}
+    dom = max(shares, key=shares.get)
+    bnd = scene.nb if dom != "cg_ap" else 0
+    algo = ALGO_BYTES[dom] * scene.n + BOUNDARY_BYTES * bnd
+    peak, src = measured_peaks()
+    achieved = algo / (per[dom] / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "dram_traffic.json"
+    if tf.exists():
+        d = json.loads(tf.read_text()).get(dom)
+        if d:
+            traffic = d.get("bytes_per_launch_full_workload")
+    step_algo = (432 + 96 * (runs[0] + runs[2]) / args.steps + 184 * runs[1] / args.steps) * scene.n + \
+        16 * scene.nb * (1 + 2 * (runs[0] + runs[2]) / args.steps)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,
+                   "kernel": "cubic spline", "dt": scene.physics["dt"],
+                   "l2": "inputs larger than L2: state + neighbour lists + CG vectors ~%.0f MB > 129 MB"
+                         % ((scene.n * (32 + 4 * 40 + 80)) / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "iterations_per_step": {"df": iters[0] / args.steps, "cg": iters[1] / args.steps, "cd": iters[2] / args.steps},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": algo, "ms_per_launch": per[dom],
+                     "ms_per_launch_all": per},
+        "step_roofline": {"algorithmic_bytes_per_step": step_algo,
+                          "achieved_gbs": step_algo / (ms_max / args.steps / 1e3) / 1e9},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(scene)
+    if dist:
+        import torch.distributed as td
+        td.destroy_process_group()
+    return line
+
+
+def run_reference(args, scene, rank, world, local_rank):
+    """The reference's own CUDA step (FP64) on rank 0."""
+    if rank != 0:
+        return None
+    from oracle import refstep
+    import ctypes
+    cudart = ctypes.CDLL("libcudart.so")
+    cudart.cudaSetDevice(local_rank)
+    try:
+        ref = refstep.RefStep(scene, variant="config")
+    except Exception as e:  # noqa: BLE001
+        return {"impl": "reference", "unavailable": f"reference step could not be set up: {e}"}
+    ref.step(args.warmup)
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        ref.step(args.steps)
+        dt = time.perf_counter() - t0
+    value = scene.n * args.steps / dt
+    loops = ref.loops()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,
+                   "kernel": "cubic spline (USE_CUBIC_KERNEL 1)", "tolerances": "1e-3 / 1e-3",
+                   "implementation": "moonsh5009/MPS_CUDA step, FP64, rebuilt headless for sm_103a",
+                   "l2": "inputs larger than L2"},
+        "last_step_loops": {"df": loops[0], "cg": loops[1], "cd": loops[2]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": None, "kind": "reference",
+                         "sample": f"{args.steps} steps of the reference's own CUDA step on the GPU (it has no CPU "
+                                   f"implementation); host wall clock around its synchronous step calls"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "clocks": clk.summary(),
+    }
+    ref.close()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="dam_break_1m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local_rank = env_rank()
+    from mps_cuda_gb300 import scenes
+    scene = scenes.CONFIGS[args.config](seed=rank) if args.config != "reference_surface_tension" else \
+        scenes.reference_surface_tension()
+    if args.impl == "reference":
+        line = run_reference(args, scene, rank, world, local_rank)
+    else:
+        line = run_ours(args, scene, rank, world, local_rank)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+/*
+ * mps_c.h -- C ABI of the GB300-native DFSPH step (libmps_gb300.so).
+ *
+ * Replaces the per-frame step of moonsh5009/MPS_CUDA: `mps::System::OnUpdate`
+ * (src/MPS_System/MPSSystem.cpp:191-291) and the free functions it calls in
+ * `mps::kernel::SPH::*` / `mps::kernel::Advect::*` (src/MPS_Computer/MPSSPHBaseUtil.h:9-38,
+ * MPSSPHDFSPHUtil.h:9-87, MPSSPHNonPressureUtil.h:29-65, MPSAdvectUtil.h:12-20) plus the
+ * neighbour search of `mps::SpatialHash` (src/MPS_Object/MPSSpatialHash.h:20-57).
+ *
+ * Conventions
+ *  - Plain C types only; every call returns MPS_OK (0) or a negative MPS_E* code, and
+ *    mps_last_error() returns a message for the calling thread's last failure.
+ *  - "particle radius" r is what the reference stores per particle (pRadius); the support
+ *    radius is h = 4 r (H_RATIO, src/MPS_Object/MPSDef.h:25-27).
+ *  - Work is queued on the stream passed in (a cudaStream_t as void*, NULL = legacy default).
+ *  - One handle is used from one host thread at a time.
+ */
+#ifndef MPS_C_H
+#define MPS_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#define MPS_ABI_VERSION 1
+
+enum mps_status {
+    MPS_OK = 0,
+    MPS_E_INVALID = -1,       /* bad argument or handle */
+    MPS_E_CUDA = -2,          /* CUDA runtime error (message in mps_last_error) */
+    MPS_E_NOMEM = -3,         /* device allocation failed */
+    MPS_E_STATE = -4,         /* call out of order (e.g. step before set_fluid) */
+    MPS_E_OVERFLOW = -5,      /* neighbour list capacity exceeded during the last step */
+    MPS_E_NONFINITE = -6      /* NaN/Inf met in particle positions during the last step */
+};
+
+/* SPHMaterialParam (src/MPS_Object/MPSSPHMaterial.h:9-21). */
+typedef struct mps_material {
+    double radius;           /* support radius h of the material (reference: SetRadius(4 r)) */
+    double mass;             /* particle mass (reference: density * volume) */
+    double density;          /* rest density rho0 */
+    double volume;           /* particle volume V used by the fluid sums */
+    double viscosity;
+    double xsph;
+    double surface_tension;
+} mps_material;
+
+/* PhysicsParam (src/MPS_Object/MPSUniformDef.h:19-25). */
+typedef struct mps_physics {
+    double dt;
+    double gravity[3];
+    double min[3];           /* collision box (BoundaryCollision, MPSAdvectUtil.cuh:48-77) */
+    double max[3];
+} mps_physics;
+
+enum mps_kernel_kind { MPS_KERNEL_POLY6_SPIKY = 0, MPS_KERNEL_CUBIC_SPLINE = 1 };
+
+/* Solver rules.  Defaults (mps_default_config) reproduce the reference's literals:
+ * MPSSPHDFSPHUtil.cu:333 (CD 1e-4, l > 2), :419 (DF 1e-3, l > 1), :299/:405 (<= 100
+ * iterations), MPSSolver.cuh:31-41 (CG r.r < 1e-2, <= 100 iterations),
+ * MPSSPHNonPressureUtil.cu:165-169 (operator factor 0 for A x0, 0.01 afterwards). */
+typedef struct mps_config {
+    int32_t kernel;              /* mps_kernel_kind */
+    double df_tol;
+    double cd_tol;
+    int32_t df_min_iter;
+    int32_t cd_min_iter;
+    int32_t max_iter;
+    double cg_tol;
+    int32_t cg_max_iter;
+    double cg_factor;
+    int32_t fixed_iters;         /* > 0: DF, CD and CG each run exactly this many iterations */
+    int32_t max_fluid_neighbors; /* list capacity per particle (overflow -> MPS_E_OVERFLOW) */
+    int32_t max_boundary_neighbors;
+    int32_t volume_accumulate;   /* 1: reproduce the un-reset boundary volume (MPSSystem.cpp:237-238) */
+    int32_t use_graph;           /* 1: whole step as one CUDA graph with device-side loops */
+    int32_t block_size;          /* threads per block of the neighbour-sum kernels (64..256) */
+} mps_config;
+
+/* Per-step statistics, written by the device at the end of each step. */
+typedef struct mps_stats {
+    int32_t df_iters;        /* reference loop counter l at exit (MPSSPHDFSPHUtil.cu:404-433) */
+    int32_t cg_iters;        /* CGSolver return value (MPSSolver.cuh:30-72) */
+    int32_t cd_iters;
+    int32_t flags;           /* bit0 neighbour overflow, bit1 non-finite position */
+    double df_err;           /* last mean divergence error */
+    double cd_err;           /* last mean density error */
+    double cg_rr;            /* last r.r */
+    int64_t fluid_pairs;     /* fluid-fluid neighbour pairs of the step */
+    int64_t boundary_pairs;  /* fluid-boundary neighbour pairs of the step */
+    int64_t steps;           /* steps taken since creation */
+    int64_t iters_total[3];  /* DF, CG, CD loop counters summed over steps (and scenes) */
+    int64_t runs_total[3];   /* DF, CG, CD loop bodies executed since creation */
+} mps_stats;
+
+typedef struct mps_handle mps_handle;
+
+const char* mps_last_error(void);
+int mps_abi_version(void);
+void mps_default_config(mps_config* cfg);
+/* Reference defaults: SPHMaterial() then SetRadius(h) (MPSSPHMaterial.cpp:4-19). */
+void mps_reference_material(double h, double density, mps_material* out);
+
+/* Object lifetime: replaces SPHModel/ObstacleModel construction (MPSSystem.cpp:22-84). */
+int mps_create(const mps_material* mat, const mps_physics* phys, const mps_config* cfg,
+               int device, mps_handle** out);
+int mps_destroy(mps_handle* h);
+int mps_set_physics(mps_handle* h, const mps_physics* phys);
+int mps_set_material(mps_handle* h, const mps_material* mat);
+
+/* Fluid particles, host FP64 AoS as the reference stores them (REAL3 pos/vel, REAL mass,
+ * REAL radius; MPSSystem.cpp:586-623).  ids may be NULL (0..n-1). */
+int mps_set_fluid(mps_handle* h, int64_t n, const double* pos3, const double* vel3,
+                  const double* mass, const double* radius, const uint32_t* ids);
+/* Boundary particles: positions and particle radii; volume NULL = Akinci volume computed on
+ * the device (ComputeBoundaryParticleVolumeSub/Final, MPSSPHBaseUtil.cu:9-53). */
+int mps_set_boundary(mps_handle* h, int64_t nb, const double* pos3, const double* radius,
+                     const double* volume);
+
+/* Native FP32 layout: pos4 = (x, y, z, particle radius), vel4 = (vx, vy, vz, mass).
+ * on_device != 0: pointers are device memory.  Order: as given (becomes particle IDs). */
+int mps_set_fluid_f32(mps_handle* h, int64_t n, const float* pos4, const float* vel4,
+                      int on_device, void* stream);
+/* Reads the fluid back in ID order (particle k of mps_set_fluid* at index k). */
+int mps_get_fluid_f32(mps_handle* h, float* pos4, float* vel4, int on_device, void* stream);
+int mps_get_fluid(mps_handle* h, double* pos3, double* vel3);
+
+/* One frame of System::OnUpdate (MPSSystem.cpp:191-291), nsteps times, queued on stream. */
+int mps_step(mps_handle* h, int32_t nsteps, void* stream);
+/* Host-buffer form: copies pos4/vel4 in, steps, copies them back (ID order). */
+int mps_step_host(mps_handle* h, float* pos4, float* vel4, int32_t nsteps, void* stream);
+int mps_get_stats(mps_handle* h, mps_stats* out, void* stream);
+
+/* Fine-grained phases of the step, in OnUpdate order (for parity tests and tools). */
+enum mps_phase {
+    MPS_PHASE_SORT = 0,          /* UpdateHash / ZSort: keys, radix sort, reorder, cell ranges */
+    MPS_PHASE_NEIGHBORS = 1,     /* BuildNeighorhood x3 (MPSSpatialHash.cu:142-218) */
+    MPS_PHASE_BVOLUME = 2,       /* ComputeBoundaryParticleVolume* (MPSSystem.cpp:237-238) */
+    MPS_PHASE_DENSITY_ALPHA = 3, /* density, colour, DFSPH factor, gravity (:240-255) */
+    MPS_PHASE_DF = 4,            /* ComputeDFSPHDivergenceFree (:257-264) */
+    MPS_PHASE_VISCST = 5,        /* ApplyImplicitViscosityNSurfaceTension (:266) */
+    MPS_PHASE_CD = 6,            /* ComputeDFSPHConstantDensity (:268-275) */
+    MPS_PHASE_ADVECT = 7         /* BoundaryCollision + UpdatePosition (:277-278) */
+};
+int mps_phase(mps_handle* h, int32_t phase, void* stream);
+
+/* Per-particle fields by name: "density","alpha","pressure","delta","aux"(2: rho, ST factor),"color"(4),
+ * "pos"(4),"vel"(4),"ids"(u32),"bvol"(boundary),"bpos"(boundary, 4),
+ * "nbr_count"(u32: fluid + boundary * 65536),"cell_key"(u64),"cg_b"(4),"cg_x"(4).
+ * order: 0 = current slot order (sorted by cell), 1 = particle ID order.
+ * Values are copied to/from host memory; count is in elements of the field's type. */
+int64_t mps_field_size(mps_handle* h, const char* name);
+int mps_get_field(mps_handle* h, const char* name, void* host_dst, int order);
+int mps_put_field(mps_handle* h, const char* name, const void* host_src, int order);
+
+/* Kernels that mps_profile_kernel can time. */
+enum mps_kernel_id {
+    MPS_K_PRESSURE_A = 0,     /* density change rate + stiffness pass of a DF/CD iteration */
+    MPS_K_PRESSURE_B = 1,     /* pressure force + velocity pass of a DF/CD iteration */
+    MPS_K_CG_AP = 2,          /* viscosity + surface tension + XSPH operator pass of a CG iteration */
+    MPS_K_DENSITY_ALPHA = 3,  /* density, colour, alpha, gravity */
+    MPS_K_BUILD_NBRS = 4,     /* neighbour lists */
+    MPS_K_SORT = 5            /* cell keys + radix sort + reorder */
+};
+/* Times `reps` back-to-back launches of one kernel of the step on the current state with CUDA
+ * events recorded on `stream`; *ms = mean milliseconds per launch.  Solver passes run in their
+ * profiling form (no loop decision) and the B pass moves velocities, so call this after the
+ * work being measured.  No counterpart in the reference (it has no device timers). */
+int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream, double* ms);
+
+/* Cell grid of the step (one scene): origin, cell size, dims. */
+int mps_get_grid(mps_handle* h, float origin[3], float* cell, int32_t dims[3]);
+
+/* ---- Batched scenes (many independent scenes, one set of launches per pass) ---- */
+/* Scenes are concatenated: fluid of scene s is particles [fluid_offsets[s], fluid_offsets[s+1])
+ * of pos4/vel4, boundary of scene s is [boundary_offsets[s], boundary_offsets[s+1]).
+ * boxes: 6 doubles per scene (min xyz, max xyz) for collision and the cell grid. */
+int mps_create_batched(const mps_material* mat, const mps_physics* phys, const mps_config* cfg,
+                       int device, int32_t nscenes, const int64_t* fluid_offsets,
+                       const int64_t* boundary_offsets, const double* boxes, mps_handle** out);
+int mps_set_batched(mps_handle* h, const float* pos4, const float* vel4, const float* bpos4,
+                    void* stream);
+int mps_get_batched(mps_handle* h, float* pos4, float* vel4, void* stream);
+/* Per-scene iteration counts of the last step: 3 int32 per scene (DF, CG, CD). */
+int mps_get_scene_iters(mps_handle* h, int32_t* out3);
+
+/* ---- Scene generation (host only, deterministic across platforms) ---- */
+/* Jittered lattice block: nx*ny*nz particles at lower corner origin + spacing*(i+1).
+ * Writes pos4 (x,y,z,radius) and vel4 (0,0,0,mass).  jitter: uniform in [-jitter, jitter]. */
+int mps_gen_block(int32_t nx, int32_t ny, int32_t nz, const double origin[3], double spacing,
+                  double radius, double mass, double jitter, uint64_t seed, float* pos4,
+                  float* vel4);
+/* Single-layer walls of an axis-aligned box at spacing (open_mask bit k: skip face k,
+ * faces ordered -x,+x,-y,+y,-z,+z).  Returns particle count; pos4 may be NULL to count. */
+int64_t mps_gen_box_walls(const double lo[3], const double hi[3], double spacing, double radius,
+                          int32_t open_mask, float* pos4);
+/* Sphere surface sampled at about spacing (Fibonacci lattice).  Returns count; pos4 may be NULL. */
+int64_t mps_gen_sphere(const double center[3], double R, double spacing, double radius, float* pos4);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPS_C_H */

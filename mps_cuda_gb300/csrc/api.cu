@@ -1,0 +1,1203 @@
+// Host side of the GB300 DFSPH step: state management, step orchestration as one CUDA graph
+// with device-side WHILE loops, and the C ABI declared in include/mps_c.h.
+//
+// Step order follows mps::System::OnUpdate (moonsh5009/MPS_CUDA src/MPS_System/MPSSystem.cpp:
+// 220-278): sort/hash, neighbour lists, boundary volume, density + colour + alpha, gravity,
+// divergence-free solve, implicit viscosity/surface tension CG, constant-density solve,
+// collision + position.  Differences of design: every step re-sorts the fluid by cell into SoA
+// float4 slots (the reference re-sorts every 50 frames); the solver loops never return to the
+// host (the reference reads the residual back once per iteration, MPSSPHDFSPHUtil.cu:331,417,
+// and three scalars per CG iteration, MPSSolver.cuh:40,54,59); no allocation happens inside a
+// step (the reference allocates r, p, Ap and residual buffers every step).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/mps_c.h"
+#include "mps_internal.cuh"
+
+using namespace mpsg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define MPS_CUDA_TRY(expr)                                                                      \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(e_ == cudaErrorMemoryAllocation ? MPS_E_NOMEM : MPS_E_CUDA,             \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+// Host copy of the FP32 cell coordinate of the device (same operations, no contraction).
+inline int host_cell(float x, float o, float inv, int dim) {
+    volatile float t = (x - o);
+    volatile float u = t * inv;
+    const float v = u;
+    if (!(v >= 0.0f)) return 0;
+    if (v >= float(dim)) return dim - 1;
+    const int c = int(v);
+    return c < dim ? c : dim - 1;
+}
+
+}  // namespace
+
+struct mps_handle {
+    int device = 0;
+    mps_material mat{};
+    mps_physics phys{};
+    mps_config cfg{};
+    bool batched = false;
+    int nscenes = 1;
+    std::vector<double> boxes;           // 6 per scene (batched); single scene uses phys
+    std::vector<int64_t> fluid_off, bnd_off;
+    std::vector<Scene> scenes;
+    int64_t n = 0, nb = 0;
+    int slots = 0;
+    unsigned long long total_cells = 0;
+    int key_bits = 0;
+    bool have_fluid = false;
+    bool have_boundary = false;
+    bool bvol_given = false;
+    bool layout_ready = false;
+    int cur = 0;                         // state buffer holding the current order
+    int64_t steps = 0;
+
+    // device memory
+    float4* pos[2] = {nullptr, nullptr};
+    float4* vel[2] = {nullptr, nullptr};
+    unsigned* ids[2] = {nullptr, nullptr};
+    unsigned long long* slot_key = nullptr;
+    uint2* ftable = nullptr;
+    uint2* btable = nullptr;
+    Scene* d_scenes = nullptr;
+    int* chunk_scene = nullptr;
+    unsigned* nbr_f = nullptr;
+    unsigned* nbr_b = nullptr;
+    unsigned* cnt = nullptr;
+    float *rho = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
+    float2* aux = nullptr;
+    float4* color = nullptr;
+    float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr;
+    float4* bpos = nullptr;
+    float* bvol = nullptr;
+    double* partial = nullptr;
+    SceneSolve* solve = nullptr;
+    StepCounters* ctr = nullptr;
+    int* scene_iters = nullptr;
+    double* scene_err = nullptr;
+    unsigned long long *keys = nullptr, *keys_tmp = nullptr;
+    unsigned *vals = nullptr, *vals_tmp = nullptr;
+    unsigned* sort_counts = nullptr;
+    float4 *stage_pos = nullptr, *stage_vel = nullptr;   // ID-order staging for I/O
+    int* h_nactive = nullptr;                            // pinned
+
+    std::vector<uint32_t> bperm;        // sorted boundary index -> user boundary index
+    std::vector<float4> bpos_user;      // boundary positions as given (x,y,z,h) in user order
+    std::vector<float> bvol_user;
+
+    cudaStream_t cap_stream = nullptr;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (cur, nsteps) -> exec
+    std::vector<cudaGraph_t> graph_defs;
+
+    ~mps_handle() { release(); if (cap_stream) { cudaStreamDestroy(cap_stream); cap_stream = nullptr; } }
+    void drop_graphs();
+    void release();   // frees every device buffer and forgets the layout
+};
+
+void mps_handle::drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    for (auto g : graph_defs) cudaGraphDestroy(g);
+    graph_defs.clear();
+}
+
+void mps_handle::release() {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    drop_graphs();
+    void** ptrs[] = {(void**)&pos[0], (void**)&pos[1], (void**)&vel[0], (void**)&vel[1], (void**)&ids[0],
+                     (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
+                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&rho,
+                     (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
+                     (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&bpos, (void**)&bvol,
+                     (void**)&partial, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
+                     (void**)&keys, (void**)&keys_tmp, (void**)&vals, (void**)&vals_tmp, (void**)&sort_counts,
+                     (void**)&stage_pos, (void**)&stage_vel};
+    for (void** q : ptrs) {
+        if (*q) cudaFree(*q);
+        *q = nullptr;
+    }
+    if (h_nactive) cudaFreeHost(h_nactive);
+    h_nactive = nullptr;
+    layout_ready = false;
+    have_fluid = false;
+    cur = 0;
+    cudaSetDevice(prev);
+}
+
+namespace {
+
+struct DeviceGuard {
+    int prev = 0;
+    explicit DeviceGuard(int dev) { cudaGetDevice(&prev); cudaSetDevice(dev); }
+    ~DeviceGuard() { cudaSetDevice(prev); }
+};
+
+Params make_params(const mps_handle* h) {
+    Params p{};
+    const auto& m = h->mat;
+    const auto& ph = h->phys;
+    const auto& c = h->cfg;
+    p.dt = float(ph.dt);
+    p.inv_dt = float(1.0 / ph.dt);
+    p.gx = float(ph.gravity[0]);
+    p.gy = float(ph.gravity[1]);
+    p.gz = float(ph.gravity[2]);
+    p.rho0 = float(m.density);
+    p.inv_rho0 = float(1.0 / m.density);
+    p.V = float(m.volume);
+    p.visc = float(m.viscosity);
+    p.xsph = float(m.xsph);
+    p.sigma = float(m.surface_tension);
+    p.cg_factor = float(c.cg_factor);
+    p.cubic = c.kernel == MPS_KERNEL_CUBIC_SPLINE ? 1 : 0;
+    p.cap_f = c.max_fluid_neighbors;
+    p.cap_b = c.max_boundary_neighbors;
+    p.slots = h->slots;
+    p.nscenes = h->nscenes;
+    p.fixed_iters = c.fixed_iters;
+    p.min_iter_df = c.df_min_iter;
+    p.min_iter_cd = c.cd_min_iter;
+    p.max_iter = c.max_iter;
+    p.cg_max_iter = c.cg_max_iter;
+    p.df_tol = float(c.df_tol);
+    p.cd_tol = float(c.cd_tol);
+    p.cg_tol = float(c.cg_tol);
+    p.df_tol_d = c.df_tol;
+    p.cd_tol_d = c.cd_tol;
+    p.cg_tol_d = c.cg_tol;
+    return p;
+}
+
+// sorted_buf: buffer that holds (or receives, for the sort) the cell-sorted state.
+Dev make_dev(const mps_handle* h, int sorted_buf) {
+    Dev d{};
+    d.pos = h->pos[sorted_buf];
+    d.vel = h->vel[sorted_buf];
+    d.ids = h->ids[sorted_buf];
+    d.pos_in = h->pos[1 - sorted_buf];
+    d.vel_in = h->vel[1 - sorted_buf];
+    d.ids_in = h->ids[1 - sorted_buf];
+    d.slot_key = h->slot_key;
+    d.ftable = h->ftable;
+    d.btable = h->btable;
+    d.scenes = h->d_scenes;
+    d.chunk_scene = h->chunk_scene;
+    d.nbr_f = h->nbr_f;
+    d.nbr_b = h->nbr_b;
+    d.cnt = h->cnt;
+    d.rho = h->rho;
+    d.alpha = h->alpha;
+    d.kappa = h->kappa;
+    d.delta = h->delta;
+    d.aux = h->aux;
+    d.color = h->color;
+    d.cg_x = h->cg_x;
+    d.cg_r = h->cg_r;
+    d.cg_p = h->cg_p;
+    d.cg_ap = h->cg_ap;
+    d.cg_b = h->cg_b;
+    d.bpos = h->bpos;
+    d.bvol = h->bvol;
+    d.partial = h->partial;
+    d.solve = h->solve;
+    d.ctr = h->ctr;
+    d.scene_iters = h->scene_iters;
+    d.scene_err = h->scene_err;
+    d.keys = h->keys;
+    d.vals = h->vals;
+    return d;
+}
+
+int block_size(const mps_handle* h) {
+    const int bs = h->cfg.block_size;
+    return (bs == 64 || bs == 128 || bs == 256) ? bs : 128;
+}
+
+// Scene layout and grids.  Grid of a scene: its box grown by one cell on every side, cell =
+// largest support radius of the scene's particles.
+int build_layout(mps_handle* h, const std::vector<float>& max_h_scene) {
+    const int S = h->nscenes;
+    h->scenes.assign(size_t(S), Scene{});
+    int64_t slot = 0, coff = 0;
+    unsigned long long key = 0;
+    for (int s = 0; s < S; ++s) {
+        Scene& sc = h->scenes[size_t(s)];
+        const double* box = h->batched ? &h->boxes[6 * size_t(s)] : nullptr;
+        const double lo[3] = {box ? box[0] : h->phys.min[0], box ? box[1] : h->phys.min[1], box ? box[2] : h->phys.min[2]};
+        const double hi[3] = {box ? box[3] : h->phys.max[0], box ? box[4] : h->phys.max[1], box ? box[5] : h->phys.max[2]};
+        const float cell = max_h_scene[size_t(s)] > 0.0f ? max_h_scene[size_t(s)] : 1.0f;
+        sc.cell = cell;
+        sc.inv_cell = 1.0f / cell;
+        int dims[3];
+        for (int a = 0; a < 3; ++a) {
+            const double ext = std::max(hi[a] - lo[a], 0.0);
+            const double nd = std::ceil(ext / double(cell)) + 2.0;
+            if (!(nd >= 1.0) || nd > 4.0e6) return fail(MPS_E_INVALID, "cell grid too large for the box; check min/max");
+            dims[a] = int(nd);
+        }
+        sc.ox = float(lo[0] - cell);
+        sc.oy = float(lo[1] - cell);
+        sc.oz = float(lo[2] - cell);
+        sc.nx = dims[0];
+        sc.ny = dims[1];
+        sc.nz = dims[2];
+        sc.key_base = key;
+        const unsigned long long cells = (unsigned long long)dims[0] * dims[1] * dims[2];
+        key += cells;
+        sc.bminx = float(lo[0]); sc.bminy = float(lo[1]); sc.bminz = float(lo[2]);
+        sc.bmaxx = float(hi[0]); sc.bmaxy = float(hi[1]); sc.bmaxz = float(hi[2]);
+        const int64_t ns = h->fluid_off[size_t(s) + 1] - h->fluid_off[size_t(s)];
+        sc.n = int(ns);
+        sc.coff = int(coff);
+        sc.slot_begin = int(slot);
+        const int64_t padded = std::max<int64_t>(kPad, (ns + kPad - 1) / kPad * kPad);
+        sc.slot_end = int(slot + padded);
+        slot += padded;
+        coff += ns;
+        sc.bbegin = int(h->bnd_off[size_t(s)]);
+        sc.bend = int(h->bnd_off[size_t(s) + 1]);
+    }
+    if (slot > (int64_t(1) << 30)) return fail(MPS_E_INVALID, "too many particles");
+    if (key > (1ull << 40)) return fail(MPS_E_INVALID, "total cell count too large");
+    h->slots = int(slot);
+    h->total_cells = key;
+    int bits = 1;
+    while ((1ull << bits) < key) bits++;
+    h->key_bits = bits;
+    return MPS_OK;
+}
+
+int allocate(mps_handle* h) {
+    DeviceGuard g(h->device);
+    const size_t S = size_t(h->slots);
+    const size_t N = size_t(std::max<int64_t>(h->n, 1));
+    for (int b = 0; b < 2; ++b) {
+        MPS_CUDA_TRY(dalloc(&h->pos[b], S));
+        MPS_CUDA_TRY(dalloc(&h->vel[b], S));
+        MPS_CUDA_TRY(dalloc(&h->ids[b], S));
+        MPS_CUDA_TRY(cudaMemset(h->pos[b], 0, S * sizeof(float4)));
+        MPS_CUDA_TRY(cudaMemset(h->vel[b], 0, S * sizeof(float4)));
+        MPS_CUDA_TRY(cudaMemset(h->ids[b], 0xff, S * sizeof(unsigned)));
+    }
+    MPS_CUDA_TRY(dalloc(&h->slot_key, S));
+    MPS_CUDA_TRY(cudaMemset(h->slot_key, 0xff, S * sizeof(unsigned long long)));
+    MPS_CUDA_TRY(dalloc(&h->ftable, size_t(h->total_cells)));
+    MPS_CUDA_TRY(cudaMemset(h->ftable, 0, size_t(h->total_cells) * sizeof(uint2)));
+    MPS_CUDA_TRY(dalloc(&h->btable, size_t(h->total_cells)));
+    MPS_CUDA_TRY(cudaMemset(h->btable, 0, size_t(h->total_cells) * sizeof(uint2)));
+    MPS_CUDA_TRY(dalloc(&h->d_scenes, size_t(h->nscenes)));
+    MPS_CUDA_TRY(cudaMemcpy(h->d_scenes, h->scenes.data(), h->scenes.size() * sizeof(Scene), cudaMemcpyHostToDevice));
+    std::vector<int> chunk(S / kChunk);
+    for (int s = 0; s < h->nscenes; ++s)
+        for (int c = h->scenes[size_t(s)].slot_begin / kChunk; c < h->scenes[size_t(s)].slot_end / kChunk; ++c) chunk[size_t(c)] = s;
+    MPS_CUDA_TRY(dalloc(&h->chunk_scene, chunk.size()));
+    MPS_CUDA_TRY(cudaMemcpy(h->chunk_scene, chunk.data(), chunk.size() * sizeof(int), cudaMemcpyHostToDevice));
+    MPS_CUDA_TRY(dalloc(&h->nbr_f, S * size_t(h->cfg.max_fluid_neighbors)));
+    MPS_CUDA_TRY(dalloc(&h->nbr_b, S * size_t(h->cfg.max_boundary_neighbors)));
+    MPS_CUDA_TRY(dalloc(&h->cnt, S));
+    MPS_CUDA_TRY(cudaMemset(h->cnt, 0, S * sizeof(unsigned)));
+    MPS_CUDA_TRY(dalloc(&h->rho, S));
+    MPS_CUDA_TRY(dalloc(&h->alpha, S));
+    MPS_CUDA_TRY(dalloc(&h->kappa, S));
+    MPS_CUDA_TRY(dalloc(&h->delta, S));
+    MPS_CUDA_TRY(dalloc(&h->aux, S));
+    MPS_CUDA_TRY(dalloc(&h->color, S));
+    float* zf[] = {h->rho, h->alpha, h->kappa, h->delta};
+    for (float* z : zf) MPS_CUDA_TRY(cudaMemset(z, 0, S * sizeof(float)));
+    MPS_CUDA_TRY(cudaMemset(h->aux, 0, S * sizeof(float2)));
+    MPS_CUDA_TRY(cudaMemset(h->color, 0, S * sizeof(float4)));
+    float4** cgv[] = {&h->cg_x, &h->cg_r, &h->cg_p, &h->cg_ap, &h->cg_b};
+    for (float4** v : cgv) {
+        MPS_CUDA_TRY(dalloc(v, S));
+        MPS_CUDA_TRY(cudaMemset(*v, 0, S * sizeof(float4)));
+    }
+    MPS_CUDA_TRY(dalloc(&h->bpos, size_t(std::max<int64_t>(h->nb, 1))));
+    MPS_CUDA_TRY(dalloc(&h->bvol, size_t(std::max<int64_t>(h->nb, 1))));
+    MPS_CUDA_TRY(dalloc(&h->partial, 2 * (S / 64 + 1)));
+    MPS_CUDA_TRY(dalloc(&h->solve, size_t(h->nscenes)));
+    MPS_CUDA_TRY(cudaMemset(h->solve, 0, size_t(h->nscenes) * sizeof(SceneSolve)));
+    MPS_CUDA_TRY(dalloc(&h->ctr, 1));
+    MPS_CUDA_TRY(cudaMemset(h->ctr, 0, sizeof(StepCounters)));
+    MPS_CUDA_TRY(dalloc(&h->scene_iters, 3 * size_t(h->nscenes)));
+    MPS_CUDA_TRY(cudaMemset(h->scene_iters, 0, 3 * size_t(h->nscenes) * sizeof(int)));
+    MPS_CUDA_TRY(dalloc(&h->scene_err, 3 * size_t(h->nscenes)));
+    MPS_CUDA_TRY(cudaMemset(h->scene_err, 0, 3 * size_t(h->nscenes) * sizeof(double)));
+    MPS_CUDA_TRY(dalloc(&h->keys, N));
+    MPS_CUDA_TRY(dalloc(&h->keys_tmp, N));
+    MPS_CUDA_TRY(dalloc(&h->vals, N));
+    MPS_CUDA_TRY(dalloc(&h->vals_tmp, N));
+    MPS_CUDA_TRY(dalloc(&h->sort_counts, radix_counts_size(int(N))));
+    MPS_CUDA_TRY(dalloc(&h->stage_pos, N));
+    MPS_CUDA_TRY(dalloc(&h->stage_vel, N));
+    MPS_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&h->h_nactive), sizeof(int)));
+    if (!h->cap_stream) MPS_CUDA_TRY(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+    h->layout_ready = true;
+    return MPS_OK;
+}
+
+// Sort the boundary by cell key on the host (static, once), build its cell table, upload.
+int upload_boundary(mps_handle* h) {
+    const int64_t nb = h->nb;
+    std::vector<unsigned long long> key(static_cast<size_t>(nb));
+    std::vector<uint32_t> ord(static_cast<size_t>(nb));
+    for (int s = 0; s < h->nscenes; ++s) {
+        const Scene& sc = h->scenes[size_t(s)];
+        for (int64_t b = sc.bbegin; b < sc.bend; ++b) {
+            const float4 x = h->bpos_user[size_t(b)];
+            const int cx = host_cell(x.x, sc.ox, sc.inv_cell, sc.nx);
+            const int cy = host_cell(x.y, sc.oy, sc.inv_cell, sc.ny);
+            const int cz = host_cell(x.z, sc.oz, sc.inv_cell, sc.nz);
+            key[size_t(b)] = sc.key_base + ((unsigned long long)cz * unsigned(sc.ny) + unsigned(cy)) * unsigned(sc.nx) + unsigned(cx);
+        }
+    }
+    std::iota(ord.begin(), ord.end(), 0u);
+    std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+    h->bperm = ord;
+    std::vector<float4> bp(static_cast<size_t>(nb));
+    std::vector<float> bv(size_t(nb), 0.0f);
+    for (int64_t k = 0; k < nb; ++k) {
+        bp[size_t(k)] = h->bpos_user[ord[size_t(k)]];
+        if (h->bvol_given) bv[size_t(k)] = h->bvol_user[ord[size_t(k)]];
+    }
+    std::vector<uint2> table(size_t(h->total_cells), make_uint2(0u, 0u));
+    for (int64_t k = 0; k < nb; ++k) {
+        const unsigned long long c = key[ord[size_t(k)]];
+        if (k == 0 || key[ord[size_t(k) - 1]] != c) table[size_t(c)].x = unsigned(k);
+        if (k == nb - 1 || key[ord[size_t(k) + 1]] != c) table[size_t(c)].y = unsigned(k + 1);
+    }
+    DeviceGuard g(h->device);
+    if (nb > 0) {
+        MPS_CUDA_TRY(cudaMemcpy(h->bpos, bp.data(), size_t(nb) * sizeof(float4), cudaMemcpyHostToDevice));
+        MPS_CUDA_TRY(cudaMemcpy(h->bvol, bv.data(), size_t(nb) * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    MPS_CUDA_TRY(cudaMemcpy(h->btable, table.data(), table.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    if (!h->bvol_given && nb > 0) {
+        const Params p = make_params(h);
+        launch_bvolume(make_dev(h, h->cur), p, int(nb), 0, nullptr);
+        MPS_CUDA_TRY(cudaGetLastError());
+        MPS_CUDA_TRY(cudaDeviceSynchronize());
+    }
+    return MPS_OK;
+}
+
+// --------------------------------------------------------------------- step launches
+int phase_sort(mps_handle* h, cudaStream_t s) {
+    const Params p = make_params(h);
+    const Dev d = make_dev(h, 1 - h->cur);
+    launch_keys(d, p, s);
+    MPS_CUDA_TRY(radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n),
+                                  h->key_bits, 8, s));
+    launch_reorder(d, p, int(h->n), s);
+    h->cur = 1 - h->cur;
+    return MPS_OK;
+}
+
+void phase_neighbors(mps_handle* h, cudaStream_t s) {
+    const Params p = make_params(h);
+    cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 2 * sizeof(unsigned long long), s);
+    launch_build_nbrs(make_dev(h, h->cur), p, block_size(h), s);
+}
+
+// Eager solver loop: one host read of the active-scene count per iteration.
+int eager_loop(mps_handle* h, cudaStream_t s, int kind /*0 DF,1 CG,2 CD*/) {
+    const Params p = make_params(h);
+    const Dev d = make_dev(h, h->cur);
+    const int bs = block_size(h);
+    const int cap = (h->cfg.fixed_iters > 0 ? h->cfg.fixed_iters : (kind == 1 ? h->cfg.cg_max_iter : h->cfg.max_iter)) + 2;
+    for (int it = 0; it < cap; ++it) {
+        if (kind == 1) {
+            launch_cg_ap(d, p, bs, 0ull, 0, s);
+            launch_cg_update(d, p, bs, s);
+            launch_cg_dir(d, p, bs, 0ull, 0, 0, s);
+        } else {
+            launch_pressure_A(d, p, kind == 0 ? 0 : 1, bs, 0ull, 0, s);
+            launch_pressure_B(d, p, bs, 0ull, 0, 0, s);
+        }
+        MPS_CUDA_TRY(cudaMemcpyAsync(h->h_nactive, &h->ctr->nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MPS_CUDA_TRY(cudaStreamSynchronize(s));
+        if (*h->h_nactive == 0) break;
+    }
+    return MPS_OK;
+}
+
+int run_phase(mps_handle* h, int phase, cudaStream_t s) {
+    const Params p = make_params(h);
+    const int bs = block_size(h);
+    switch (phase) {
+        case MPS_PHASE_SORT: return phase_sort(h, s);
+        case MPS_PHASE_NEIGHBORS: phase_neighbors(h, s); break;
+        case MPS_PHASE_BVOLUME:
+            if (h->cfg.volume_accumulate) launch_bvolume(make_dev(h, h->cur), p, int(h->nb), 1, s);
+            break;
+        case MPS_PHASE_DENSITY_ALPHA: launch_density_alpha(make_dev(h, h->cur), p, bs, s); break;
+        case MPS_PHASE_DF:
+        case MPS_PHASE_CD: {
+            const Dev d = make_dev(h, h->cur);
+            launch_solver_init(d, p, s);
+            const int r = eager_loop(h, s, phase == MPS_PHASE_DF ? 0 : 2);
+            if (r) return r;
+            launch_solver_finish(d, p, phase == MPS_PHASE_DF ? 0 : 2, s);
+            break;
+        }
+        case MPS_PHASE_VISCST: {
+            const Dev d = make_dev(h, h->cur);
+            launch_st_factor(d, p, bs, s);
+            launch_cg_b(d, p, bs, s);
+            launch_cg_ax0(d, p, bs, s);
+            launch_solver_init(d, p, s);
+            const int r = eager_loop(h, s, 1);
+            if (r) return r;
+            launch_solver_finish(d, p, 1, s);
+            launch_cg_finish(d, p, s);
+            break;
+        }
+        case MPS_PHASE_ADVECT: launch_advect(make_dev(h, h->cur), p, s); break;
+        default: return fail(MPS_E_INVALID, "unknown phase");
+    }
+    MPS_CUDA_TRY(cudaGetLastError());
+    return MPS_OK;
+}
+
+// ------------------------------------------------------------------ graph capture
+// Hard bound on the loop bodies of one device-side solve (kind 0 DF, 1 CG, 2 CD): the decision
+// logic ends a loop after at most the iteration cap; this guard ends it two passes later even
+// if that logic failed, and flags the step (bit 2).
+int loop_limit(const mps_handle* h, int kind) {
+    const int cap = h->cfg.fixed_iters > 0 ? h->cfg.fixed_iters : (kind == 1 ? h->cfg.cg_max_iter : h->cfg.max_iter);
+    return cap + 2;
+}
+
+struct Capture {
+    cudaGraph_t g;
+    cudaStream_t s;
+    std::vector<cudaGraphNode_t> deps;
+};
+
+cudaError_t seg_begin(Capture& c) {
+    return cudaStreamBeginCaptureToGraph(c.s, c.g, c.deps.empty() ? nullptr : c.deps.data(), nullptr,
+                                         c.deps.size(), cudaStreamCaptureModeThreadLocal);
+}
+
+cudaError_t seg_end(Capture& c) {
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t* nd = nullptr;
+    size_t nn = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(c.s, &st, nullptr, nullptr, &nd, nullptr, &nn);
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> frontier(nd, nd + nn);
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(c.s, &out);
+    if (e != cudaSuccess) return e;
+    c.deps = frontier;
+    return cudaSuccess;
+}
+
+// Creates the condition handle of a WHILE node (default 0 at each launch; set on the device).
+cudaError_t add_while(Capture& c, unsigned long long* handle_out) {
+    cudaGraphConditionalHandle handle;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&handle, c.g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    *handle_out = handle;
+    return cudaSuccess;
+}
+
+cudaError_t add_while_node(Capture& c, unsigned long long handle, cudaGraph_t* body) {
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = handle;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    cudaError_t e = cudaGraphAddNode(&node, c.g, c.deps.empty() ? nullptr : c.deps.data(), nullptr, c.deps.size(), &np);
+    if (e != cudaSuccess) return e;
+    *body = np.conditional.phGraph_out[0];
+    c.deps.assign(1, node);
+    return cudaSuccess;
+}
+
+#define MPS_CAP_TRY(expr)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess) return e_;                                                   \
+    } while (0)
+
+// Captures nsteps steps starting from state buffer `cur` into graph g.
+cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
+    Capture c{g, h->cap_stream, {}};
+    const Params p = make_params(h);
+    const int bs = block_size(h);
+    for (int k = 0; k < nsteps; ++k) {
+        const int sorted = 1 - cur;
+        const Dev d = make_dev(h, sorted);
+        unsigned long long hdf, hcg, hcd;
+        MPS_CAP_TRY(add_while(c, &hdf));
+        MPS_CAP_TRY(add_while(c, &hcg));
+        MPS_CAP_TRY(add_while(c, &hcd));
+        // sort + neighbours + density/alpha + gravity, then DF loop set-up
+        MPS_CAP_TRY(seg_begin(c));
+        launch_keys(d, p, c.s);
+        MPS_CAP_TRY(radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, 8, c.s));
+        launch_reorder(d, p, int(h->n), c.s);
+        MPS_CAP_TRY(cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 2 * sizeof(unsigned long long), c.s));
+        launch_build_nbrs(d, p, bs, c.s);
+        if (h->cfg.volume_accumulate) launch_bvolume(d, p, int(h->nb), 1, c.s);
+        launch_density_alpha(d, p, bs, c.s);
+        launch_solver_init(d, p, c.s);
+        launch_set_cond(d, hdf, c.s);
+        MPS_CAP_TRY(cudaGetLastError());
+        MPS_CAP_TRY(seg_end(c));
+        cudaGraph_t body;
+        MPS_CAP_TRY(add_while_node(c, hdf, &body));
+        {
+            Capture b{body, h->cap_stream, {}};
+            MPS_CAP_TRY(seg_begin(b));
+            launch_pressure_A(d, p, 0, bs, hdf, 1, b.s);
+            launch_pressure_B(d, p, bs, hdf, 1, loop_limit(h, 0), b.s);
+            MPS_CAP_TRY(cudaGetLastError());
+            MPS_CAP_TRY(seg_end(b));
+        }
+        // viscosity + surface tension
+        MPS_CAP_TRY(seg_begin(c));
+        launch_solver_finish(d, p, 0, c.s);
+        launch_st_factor(d, p, bs, c.s);
+        launch_cg_b(d, p, bs, c.s);
+        launch_cg_ax0(d, p, bs, c.s);
+        launch_solver_init(d, p, c.s);
+        launch_set_cond(d, hcg, c.s);
+        MPS_CAP_TRY(cudaGetLastError());
+        MPS_CAP_TRY(seg_end(c));
+        MPS_CAP_TRY(add_while_node(c, hcg, &body));
+        {
+            Capture b{body, h->cap_stream, {}};
+            MPS_CAP_TRY(seg_begin(b));
+            launch_cg_ap(d, p, bs, hcg, 1, b.s);
+            launch_cg_update(d, p, bs, b.s);
+            launch_cg_dir(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+            MPS_CAP_TRY(cudaGetLastError());
+            MPS_CAP_TRY(seg_end(b));
+        }
+        // constant density
+        MPS_CAP_TRY(seg_begin(c));
+        launch_solver_finish(d, p, 1, c.s);
+        launch_cg_finish(d, p, c.s);
+        launch_solver_init(d, p, c.s);
+        launch_set_cond(d, hcd, c.s);
+        MPS_CAP_TRY(cudaGetLastError());
+        MPS_CAP_TRY(seg_end(c));
+        MPS_CAP_TRY(add_while_node(c, hcd, &body));
+        {
+            Capture b{body, h->cap_stream, {}};
+            MPS_CAP_TRY(seg_begin(b));
+            launch_pressure_A(d, p, 1, bs, hcd, 1, b.s);
+            launch_pressure_B(d, p, bs, hcd, 1, loop_limit(h, 2), b.s);
+            MPS_CAP_TRY(cudaGetLastError());
+            MPS_CAP_TRY(seg_end(b));
+        }
+        MPS_CAP_TRY(seg_begin(c));
+        launch_solver_finish(d, p, 2, c.s);
+        launch_advect(d, p, c.s);
+        MPS_CAP_TRY(cudaGetLastError());
+        MPS_CAP_TRY(seg_end(c));
+        cur = sorted;
+    }
+    return cudaSuccess;
+}
+
+int get_graph(mps_handle* h, int nsteps, cudaGraphExec_t* out) {
+    const auto key = std::make_pair(h->cur, nsteps);
+    auto it = h->graphs.find(key);
+    if (it != h->graphs.end()) { *out = it->second; return MPS_OK; }
+    cudaGraph_t g;
+    MPS_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaError_t e = capture_steps(h, g, h->cur, nsteps);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        cudaGetLastError();
+        return fail(MPS_E_CUDA, std::string("graph capture failed: ") + cudaGetErrorString(e));
+    }
+    cudaGraphExec_t ex;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(MPS_E_CUDA, std::string("graph instantiate failed: ") + cudaGetErrorString(e));
+    }
+    h->graph_defs.push_back(g);
+    h->graphs[key] = ex;
+    *out = ex;
+    return MPS_OK;
+}
+
+int step_eager(mps_handle* h, cudaStream_t s) {
+    for (int ph = MPS_PHASE_SORT; ph <= MPS_PHASE_ADVECT; ++ph) {
+        const int r = run_phase(h, ph, s);
+        if (r) return r;
+    }
+    return MPS_OK;
+}
+
+int check_ready(mps_handle* h) {
+    if (!h) return fail(MPS_E_INVALID, "null handle");
+    if (!h->have_fluid || !h->layout_ready) return fail(MPS_E_STATE, "fluid not set");
+    return MPS_OK;
+}
+
+// Field table for get/put.
+struct FieldInfo {
+    void* base;
+    size_t elem;       // bytes per element
+    int comps;         // elements per particle
+    bool boundary;
+};
+
+bool field_info(mps_handle* h, const std::string& n, FieldInfo& f) {
+    const int c = h->cur;
+    if (n == "density") f = {h->rho, 4, 1, false};
+    else if (n == "alpha") f = {h->alpha, 4, 1, false};
+    else if (n == "pressure") f = {h->kappa, 4, 1, false};
+    else if (n == "delta") f = {h->delta, 4, 1, false};
+    else if (n == "aux") f = {h->aux, 4, 2, false};
+    else if (n == "color") f = {h->color, 4, 4, false};
+    else if (n == "pos") f = {h->pos[c], 4, 4, false};
+    else if (n == "vel") f = {h->vel[c], 4, 4, false};
+    else if (n == "ids") f = {h->ids[c], 4, 1, false};
+    else if (n == "nbr_count") f = {h->cnt, 4, 1, false};
+    else if (n == "cell_key") f = {h->slot_key, 8, 1, false};
+    else if (n == "cg_b") f = {h->cg_b, 4, 4, false};
+    else if (n == "cg_x") f = {h->cg_x, 4, 4, false};
+    else if (n == "bvol") f = {h->bvol, 4, 1, true};
+    else if (n == "bpos") f = {h->bpos, 4, 4, true};
+    else return false;
+    return true;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char* mps_last_error(void) { return g_last_error.c_str(); }
+int mps_abi_version(void) { return MPS_ABI_VERSION; }
+
+void mps_default_config(mps_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->kernel = MPS_KERNEL_POLY6_SPIKY;
+    c->df_tol = 1.0e-3;
+    c->cd_tol = 1.0e-4;
+    c->df_min_iter = 1;
+    c->cd_min_iter = 2;
+    c->max_iter = 100;
+    c->cg_tol = 1.0e-2;
+    c->cg_max_iter = 100;
+    c->cg_factor = 0.01;
+    c->fixed_iters = 0;
+    c->max_fluid_neighbors = 96;
+    c->max_boundary_neighbors = 64;
+    c->volume_accumulate = 0;
+    c->use_graph = 1;
+    c->block_size = 128;
+}
+
+// SPHMaterial() + SetRadius(h): V = h^3 / 48 * 3.141592, mass = density * V
+// (MPSSPHMaterial.cpp:4-19; the truncated pi is the reference's literal).
+void mps_reference_material(double h, double density, mps_material* m) {
+    m->radius = h;
+    m->volume = h * h * h / 48.0 * 3.141592;
+    m->density = density;
+    m->mass = density * m->volume;
+    m->viscosity = 0.025;
+    m->xsph = 0.1;
+    m->surface_tension = 100.0;
+}
+
+static int create_common(const mps_material* mat, const mps_physics* phys, const mps_config* cfg, int device,
+                         mps_handle** out) {
+    if (!mat || !phys || !out) return fail(MPS_E_INVALID, "null argument");
+    if (!(phys->dt > 0.0)) return fail(MPS_E_INVALID, "dt must be positive");
+    if (!(mat->density > 0.0) || !(mat->volume > 0.0)) return fail(MPS_E_INVALID, "density and volume must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(MPS_E_CUDA, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev) return fail(MPS_E_INVALID, "bad device index");
+    auto* h = new mps_handle();
+    h->device = device;
+    h->mat = *mat;
+    h->phys = *phys;
+    if (cfg) h->cfg = *cfg; else mps_default_config(&h->cfg);
+    if (h->cfg.max_fluid_neighbors <= 0 || h->cfg.max_fluid_neighbors > 65535) h->cfg.max_fluid_neighbors = 96;
+    if (h->cfg.max_boundary_neighbors <= 0 || h->cfg.max_boundary_neighbors > 65535) h->cfg.max_boundary_neighbors = 64;
+    if (h->cfg.max_iter <= 0) h->cfg.max_iter = 100;
+    if (h->cfg.cg_max_iter <= 0) h->cfg.cg_max_iter = 100;
+    *out = h;
+    return MPS_OK;
+}
+
+int mps_create(const mps_material* mat, const mps_physics* phys, const mps_config* cfg, int device, mps_handle** out) {
+    const int r = create_common(mat, phys, cfg, device, out);
+    if (r) return r;
+    (*out)->nscenes = 1;
+    return MPS_OK;
+}
+
+int mps_destroy(mps_handle* h) {
+    if (!h) return fail(MPS_E_INVALID, "null handle");
+    delete h;
+    return MPS_OK;
+}
+
+int mps_set_physics(mps_handle* h, const mps_physics* phys) {
+    if (!h || !phys || !(phys->dt > 0.0)) return fail(MPS_E_INVALID, "bad physics");
+    h->phys = *phys;
+    DeviceGuard g(h->device);
+    h->drop_graphs();
+    if (h->layout_ready && !h->batched) {
+        for (auto& sc : h->scenes) {
+            sc.bminx = float(phys->min[0]); sc.bminy = float(phys->min[1]); sc.bminz = float(phys->min[2]);
+            sc.bmaxx = float(phys->max[0]); sc.bmaxy = float(phys->max[1]); sc.bmaxz = float(phys->max[2]);
+        }
+        MPS_CUDA_TRY(cudaMemcpy(h->d_scenes, h->scenes.data(), h->scenes.size() * sizeof(Scene), cudaMemcpyHostToDevice));
+    }
+    return MPS_OK;
+}
+
+int mps_set_material(mps_handle* h, const mps_material* mat) {
+    if (!h || !mat || !(mat->density > 0.0) || !(mat->volume > 0.0)) return fail(MPS_E_INVALID, "bad material");
+    h->mat = *mat;
+    DeviceGuard g(h->device);
+    h->drop_graphs();
+    return MPS_OK;
+}
+
+// Common fluid + boundary set-up for one scene from FP32 (x,y,z,r) arrays in host memory.
+static int setup_single(mps_handle* h, int64_t n, const float4* pos4, const float4* vel4) {
+    if (h->batched) return fail(MPS_E_STATE, "batched handle: use mps_set_batched");
+    DeviceGuard g(h->device);
+    const bool relayout = !h->layout_ready || n != h->n;
+    if (relayout) {
+        h->release();
+        h->n = n;
+        h->nb = int64_t(h->bpos_user.size());
+        h->nscenes = 1;
+        h->fluid_off = {0, n};
+        h->bnd_off = {0, h->nb};
+        float maxh = 0.0f;
+        for (int64_t i = 0; i < n; ++i) maxh = std::max(maxh, pos4[i].w * kHRatio);
+        for (const auto& b : h->bpos_user) maxh = std::max(maxh, b.w);
+        std::vector<float> mh(1, maxh);
+        int r = build_layout(h, mh);
+        if (r) return r;
+        r = allocate(h);
+        if (r) return r;
+        r = upload_boundary(h);
+        if (r) return r;
+    }
+    float4* dpos;
+    float4* dvel;
+    MPS_CUDA_TRY(cudaMalloc(&dpos, size_t(std::max<int64_t>(n, 1)) * sizeof(float4)));
+    MPS_CUDA_TRY(cudaMalloc(&dvel, size_t(std::max<int64_t>(n, 1)) * sizeof(float4)));
+    cudaMemcpy(dpos, pos4, size_t(n) * sizeof(float4), cudaMemcpyHostToDevice);
+    cudaMemcpy(dvel, vel4, size_t(n) * sizeof(float4), cudaMemcpyHostToDevice);
+    const Params p = make_params(h);
+    launch_load_state(make_dev(h, h->cur), p, dpos, dvel, int(n), nullptr);
+    cudaError_t e = cudaDeviceSynchronize();
+    cudaFree(dpos);
+    cudaFree(dvel);
+    MPS_CUDA_TRY(e);
+    h->have_fluid = true;
+    return MPS_OK;
+}
+
+int mps_set_fluid(mps_handle* h, int64_t n, const double* pos3, const double* vel3, const double* mass,
+                  const double* radius, const uint32_t* ids) {
+    if (!h || n <= 0 || !pos3 || !vel3 || !mass || !radius) return fail(MPS_E_INVALID, "bad fluid arguments");
+    if (ids) {
+        for (int64_t i = 0; i < n; ++i)
+            if (ids[i] != uint32_t(i)) return fail(MPS_E_INVALID, "ids must be 0..n-1 in this version");
+    }
+    std::vector<float4> p4(static_cast<size_t>(n)), v4(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        p4[size_t(i)] = make_float4(float(pos3[3 * i]), float(pos3[3 * i + 1]), float(pos3[3 * i + 2]), float(radius[i]));
+        v4[size_t(i)] = make_float4(float(vel3[3 * i]), float(vel3[3 * i + 1]), float(vel3[3 * i + 2]), float(mass[i]));
+    }
+    return setup_single(h, n, p4.data(), v4.data());
+}
+
+int mps_set_boundary(mps_handle* h, int64_t nb, const double* pos3, const double* radius, const double* volume) {
+    if (!h || nb < 0 || (nb > 0 && (!pos3 || !radius))) return fail(MPS_E_INVALID, "bad boundary arguments");
+    if (h->batched) return fail(MPS_E_STATE, "batched handle: use mps_set_batched");
+    h->bpos_user.resize(static_cast<size_t>(nb));
+    for (int64_t i = 0; i < nb; ++i)
+        h->bpos_user[size_t(i)] = make_float4(float(pos3[3 * i]), float(pos3[3 * i + 1]), float(pos3[3 * i + 2]), float(radius[i]) * kHRatio);
+    h->bvol_given = volume != nullptr;
+    h->bvol_user.assign(size_t(nb), 0.0f);
+    if (volume)
+        for (int64_t i = 0; i < nb; ++i) h->bvol_user[size_t(i)] = float(volume[i]);
+    h->have_boundary = true;
+    if (h->layout_ready) {
+        // re-layout with the new boundary while keeping the fluid
+        std::vector<float4> p4(static_cast<size_t>(h->n)), v4(static_cast<size_t>(h->n));
+        const int r = mps_get_fluid_f32(h, reinterpret_cast<float*>(p4.data()), reinterpret_cast<float*>(v4.data()), 0, nullptr);
+        if (r) return r;
+        const int64_t n = h->n;
+        h->release();
+        return setup_single(h, n, p4.data(), v4.data());
+    }
+    return MPS_OK;
+}
+
+int mps_set_fluid_f32(mps_handle* h, int64_t n, const float* pos4, const float* vel4, int on_device, void* stream) {
+    if (!h || n <= 0 || !pos4 || !vel4) return fail(MPS_E_INVALID, "bad fluid arguments");
+    if (!h->layout_ready || n != h->n) {
+        if (h->batched) return fail(MPS_E_STATE, "batched handle: call mps_set_batched first");
+        if (on_device) return fail(MPS_E_STATE, "first set of a layout must come from host memory");
+        return setup_single(h, n, reinterpret_cast<const float4*>(pos4), reinterpret_cast<const float4*>(vel4));
+    }
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const float4* sp = reinterpret_cast<const float4*>(pos4);
+    const float4* sv = reinterpret_cast<const float4*>(vel4);
+    if (!on_device) {
+        MPS_CUDA_TRY(cudaMemcpyAsync(h->stage_pos, pos4, size_t(n) * sizeof(float4), cudaMemcpyHostToDevice, s));
+        MPS_CUDA_TRY(cudaMemcpyAsync(h->stage_vel, vel4, size_t(n) * sizeof(float4), cudaMemcpyHostToDevice, s));
+        sp = h->stage_pos;
+        sv = h->stage_vel;
+    }
+    launch_load_state(make_dev(h, h->cur), make_params(h), sp, sv, int(n), s);
+    MPS_CUDA_TRY(cudaGetLastError());
+    h->have_fluid = true;
+    return MPS_OK;
+}
+
+int mps_get_fluid_f32(mps_handle* h, float* pos4, float* vel4, int on_device, void* stream) {
+    const int r = check_ready(h);
+    if (r) return r;
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float4* dp = on_device ? reinterpret_cast<float4*>(pos4) : (pos4 ? h->stage_pos : nullptr);
+    float4* dv = on_device ? reinterpret_cast<float4*>(vel4) : (vel4 ? h->stage_vel : nullptr);
+    launch_store_state(make_dev(h, h->cur), make_params(h), dp, dv, s);
+    MPS_CUDA_TRY(cudaGetLastError());
+    if (!on_device) {
+        if (pos4) MPS_CUDA_TRY(cudaMemcpyAsync(pos4, h->stage_pos, size_t(h->n) * sizeof(float4), cudaMemcpyDeviceToHost, s));
+        if (vel4) MPS_CUDA_TRY(cudaMemcpyAsync(vel4, h->stage_vel, size_t(h->n) * sizeof(float4), cudaMemcpyDeviceToHost, s));
+        MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return MPS_OK;
+}
+
+int mps_get_fluid(mps_handle* h, double* pos3, double* vel3) {
+    const int r0 = check_ready(h);
+    if (r0) return r0;
+    std::vector<float4> p4(static_cast<size_t>(h->n)), v4(static_cast<size_t>(h->n));
+    const int r = mps_get_fluid_f32(h, reinterpret_cast<float*>(p4.data()), reinterpret_cast<float*>(v4.data()), 0, nullptr);
+    if (r) return r;
+    for (int64_t i = 0; i < h->n; ++i) {
+        if (pos3) { pos3[3 * i] = p4[size_t(i)].x; pos3[3 * i + 1] = p4[size_t(i)].y; pos3[3 * i + 2] = p4[size_t(i)].z; }
+        if (vel3) { vel3[3 * i] = v4[size_t(i)].x; vel3[3 * i + 1] = v4[size_t(i)].y; vel3[3 * i + 2] = v4[size_t(i)].z; }
+    }
+    return MPS_OK;
+}
+
+int mps_step(mps_handle* h, int32_t nsteps, void* stream) {
+    const int r = check_ready(h);
+    if (r) return r;
+    if (nsteps < 0) return fail(MPS_E_INVALID, "nsteps < 0");
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!h->cfg.use_graph) {
+        for (int k = 0; k < nsteps; ++k) {
+            const int e = step_eager(h, s);
+            if (e) return e;
+            h->steps++;
+        }
+        return MPS_OK;
+    }
+    // one graph per step; graphs for both buffer parities are cached
+    for (int k = 0; k < nsteps; ++k) {
+        cudaGraphExec_t ex;
+        const int e = get_graph(h, 1, &ex);
+        if (e) return e;
+        MPS_CUDA_TRY(cudaGraphLaunch(ex, s));
+        h->cur = 1 - h->cur;
+        h->steps++;
+    }
+    return MPS_OK;
+}
+
+int mps_step_host(mps_handle* h, float* pos4, float* vel4, int32_t nsteps, void* stream) {
+    int r = mps_set_fluid_f32(h, h ? h->n : 0, pos4, vel4, 0, stream);
+    if (r) return r;
+    r = mps_step(h, nsteps, stream);
+    if (r) return r;
+    return mps_get_fluid_f32(h, pos4, vel4, 0, stream);
+}
+
+int mps_phase(mps_handle* h, int32_t phase, void* stream) {
+    const int r = check_ready(h);
+    if (r) return r;
+    DeviceGuard g(h->device);
+    const int e = run_phase(h, phase, static_cast<cudaStream_t>(stream));
+    if (e) return e;
+    if (phase == MPS_PHASE_ADVECT) h->steps++;
+    return MPS_OK;
+}
+
+int mps_get_stats(mps_handle* h, mps_stats* out, void* stream) {
+    const int r = check_ready(h);
+    if (r) return r;
+    if (!out) return fail(MPS_E_INVALID, "null stats");
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    StepCounters c;
+    std::vector<int> it(3 * size_t(h->nscenes));
+    std::vector<double> er(3 * size_t(h->nscenes));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&c, h->ctr, sizeof(c), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(it.data(), h->scene_iters, it.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(er.data(), h->scene_err, er.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    std::memset(out, 0, sizeof(*out));
+    for (int sc = 0; sc < h->nscenes; ++sc) {
+        out->df_iters = std::max(out->df_iters, it[3 * size_t(sc)]);
+        out->cg_iters = std::max(out->cg_iters, it[3 * size_t(sc) + 1]);
+        out->cd_iters = std::max(out->cd_iters, it[3 * size_t(sc) + 2]);
+    }
+    out->df_err = er[0];
+    out->cg_rr = er[1];
+    out->cd_err = er[2];
+    out->flags = c.flags;
+    out->fluid_pairs = int64_t(c.fluid_pairs);
+    out->boundary_pairs = int64_t(c.boundary_pairs);
+    out->steps = h->steps;
+    for (int k = 0; k < 3; ++k) {
+        out->iters_total[k] = int64_t(c.iters_total[k]);
+        out->runs_total[k] = int64_t(c.runs_total[k]);
+    }
+    if (c.flags & 1) return fail(MPS_E_OVERFLOW, "neighbour list capacity exceeded");
+    if (c.flags & 2) return fail(MPS_E_NONFINITE, "non-finite particle position");
+    if (c.flags & 4) return fail(MPS_E_STATE, "a device solver loop ran past its iteration bound");
+    return MPS_OK;
+}
+
+int64_t mps_field_size(mps_handle* h, const char* name) {
+    if (!h || !name || !h->layout_ready) return -1;
+    FieldInfo f;
+    if (!field_info(h, name, f)) return -1;
+    return (f.boundary ? h->nb : h->n) * f.comps;
+}
+
+// Copies a field to the host in slot order (real slots only) or particle-ID order.
+int mps_get_field(mps_handle* h, const char* name, void* dst, int order) {
+    const int r = check_ready(h);
+    if (r) return r;
+    FieldInfo f;
+    if (!name || !dst || !field_info(h, name, f)) return fail(MPS_E_INVALID, "unknown field");
+    DeviceGuard g(h->device);
+    const size_t pe = f.elem * size_t(f.comps);
+    if (f.boundary) {
+        std::vector<unsigned char> tmp(size_t(h->nb) * pe);
+        if (h->nb) MPS_CUDA_TRY(cudaMemcpy(tmp.data(), f.base, tmp.size(), cudaMemcpyDeviceToHost));
+        auto* out = static_cast<unsigned char*>(dst);
+        for (int64_t k = 0; k < h->nb; ++k) {
+            const size_t to = order ? size_t(h->bperm[size_t(k)]) : size_t(k);
+            std::memcpy(out + to * pe, tmp.data() + size_t(k) * pe, pe);
+        }
+        return MPS_OK;
+    }
+    std::vector<unsigned char> tmp(size_t(h->slots) * pe);
+    std::vector<unsigned> ids(static_cast<size_t>(h->slots));
+    MPS_CUDA_TRY(cudaDeviceSynchronize());
+    MPS_CUDA_TRY(cudaMemcpy(tmp.data(), f.base, tmp.size(), cudaMemcpyDeviceToHost));
+    MPS_CUDA_TRY(cudaMemcpy(ids.data(), h->ids[h->cur], ids.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    auto* out = static_cast<unsigned char*>(dst);
+    int64_t k = 0;
+    for (const auto& sc : h->scenes)
+        for (int sl = sc.slot_begin; sl < sc.slot_begin + sc.n; ++sl, ++k) {
+            const size_t to = order ? size_t(ids[size_t(sl)]) : size_t(k);
+            std::memcpy(out + to * pe, tmp.data() + size_t(sl) * pe, pe);
+        }
+    return MPS_OK;
+}
+
+int mps_put_field(mps_handle* h, const char* name, const void* src, int order) {
+    const int r = check_ready(h);
+    if (r) return r;
+    FieldInfo f;
+    if (!name || !src || !field_info(h, name, f)) return fail(MPS_E_INVALID, "unknown field");
+    DeviceGuard g(h->device);
+    const size_t pe = f.elem * size_t(f.comps);
+    const auto* in = static_cast<const unsigned char*>(src);
+    if (f.boundary) {
+        std::vector<unsigned char> tmp(size_t(h->nb) * pe);
+        for (int64_t k = 0; k < h->nb; ++k) {
+            const size_t from = order ? size_t(h->bperm[size_t(k)]) : size_t(k);
+            std::memcpy(tmp.data() + size_t(k) * pe, in + from * pe, pe);
+        }
+        if (h->nb) MPS_CUDA_TRY(cudaMemcpy(f.base, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
+        return MPS_OK;
+    }
+    std::vector<unsigned char> tmp(size_t(h->slots) * pe);
+    std::vector<unsigned> ids(static_cast<size_t>(h->slots));
+    MPS_CUDA_TRY(cudaDeviceSynchronize());
+    MPS_CUDA_TRY(cudaMemcpy(tmp.data(), f.base, tmp.size(), cudaMemcpyDeviceToHost));
+    MPS_CUDA_TRY(cudaMemcpy(ids.data(), h->ids[h->cur], ids.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    int64_t k = 0;
+    for (const auto& sc : h->scenes)
+        for (int sl = sc.slot_begin; sl < sc.slot_begin + sc.n; ++sl, ++k) {
+            const size_t from = order ? size_t(ids[size_t(sl)]) : size_t(k);
+            std::memcpy(tmp.data() + size_t(sl) * pe, in + from * pe, pe);
+        }
+    MPS_CUDA_TRY(cudaMemcpy(f.base, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
+    return MPS_OK;
+}
+
+int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream, double* ms) {
+    const int r = check_ready(h);
+    if (r) return r;
+    if (!ms || reps <= 0) return fail(MPS_E_INVALID, "bad profile arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const Params p = make_params(h);
+    const Dev d = make_dev(h, h->cur);
+    const int bs = block_size(h);
+    cudaEvent_t e0, e1;
+    MPS_CUDA_TRY(cudaEventCreate(&e0));
+    MPS_CUDA_TRY(cudaEventCreate(&e1));
+    MPS_CUDA_TRY(cudaEventRecord(e0, s));
+    for (int k = 0; k < reps; ++k) {
+        switch (kernel) {
+            case MPS_K_PRESSURE_A: launch_pressure_A(d, p, 1, bs, 0ull, 2, s); break;
+            case MPS_K_PRESSURE_B: launch_pressure_B_profile(d, p, bs, s); break;
+            case MPS_K_CG_AP: launch_cg_ap(d, p, bs, 0ull, 2, s); break;
+            case MPS_K_DENSITY_ALPHA: launch_density_alpha(d, p, bs, s); break;
+            case MPS_K_BUILD_NBRS: launch_build_nbrs(d, p, bs, s); break;
+            case MPS_K_SORT: {
+                // re-sort the current order in place: keys from buffer cur, reorder into the other
+                const Dev ds = make_dev(h, 1 - h->cur);
+                launch_keys(ds, p, s);
+                radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, 8, s);
+                launch_reorder(ds, p, int(h->n), s);
+                h->cur = 1 - h->cur;
+                break;
+            }
+            default:
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return fail(MPS_E_INVALID, "unknown kernel id");
+        }
+    }
+    MPS_CUDA_TRY(cudaEventRecord(e1, s));
+    MPS_CUDA_TRY(cudaEventSynchronize(e1));
+    float t = 0.0f;
+    MPS_CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    MPS_CUDA_TRY(cudaGetLastError());
+    *ms = double(t) / reps;
+    return MPS_OK;
+}
+
+int mps_get_grid(mps_handle* h, float origin[3], float* cell, int32_t dims[3]) {
+    if (!h || !h->layout_ready) return fail(MPS_E_STATE, "no layout");
+    const Scene& sc = h->scenes[0];
+    if (origin) { origin[0] = sc.ox; origin[1] = sc.oy; origin[2] = sc.oz; }
+    if (cell) *cell = sc.cell;
+    if (dims) { dims[0] = sc.nx; dims[1] = sc.ny; dims[2] = sc.nz; }
+    return MPS_OK;
+}
+
+// ------------------------------------------------------------------ batched scenes
+int mps_create_batched(const mps_material* mat, const mps_physics* phys, const mps_config* cfg, int device,
+                       int32_t nscenes, const int64_t* fo, const int64_t* bo, const double* boxes, mps_handle** out) {
+    if (nscenes <= 0 || !fo || !bo || !boxes) return fail(MPS_E_INVALID, "bad batched arguments");
+    for (int s = 0; s < nscenes; ++s)
+        if (fo[s + 1] < fo[s] || bo[s + 1] < bo[s]) return fail(MPS_E_INVALID, "offsets must be non-decreasing");
+    const int r = create_common(mat, phys, cfg, device, out);
+    if (r) return r;
+    mps_handle* h = *out;
+    h->batched = true;
+    h->nscenes = nscenes;
+    h->fluid_off.assign(fo, fo + nscenes + 1);
+    h->bnd_off.assign(bo, bo + nscenes + 1);
+    h->boxes.assign(boxes, boxes + 6 * size_t(nscenes));
+    h->n = fo[nscenes] - fo[0];
+    h->nb = bo[nscenes] - bo[0];
+    return MPS_OK;
+}
+
+int mps_set_batched(mps_handle* h, const float* pos4, const float* vel4, const float* bpos4, void* stream) {
+    if (!h || !h->batched || !pos4 || !vel4) return fail(MPS_E_INVALID, "bad batched set");
+    DeviceGuard g(h->device);
+    const float4* p4 = reinterpret_cast<const float4*>(pos4);
+    const float4* b4 = reinterpret_cast<const float4*>(bpos4);
+    if (!h->layout_ready) {
+        std::vector<float> mh(size_t(h->nscenes), 0.0f);
+        for (int s = 0; s < h->nscenes; ++s) {
+            for (int64_t i = h->fluid_off[size_t(s)]; i < h->fluid_off[size_t(s) + 1]; ++i) mh[size_t(s)] = std::max(mh[size_t(s)], p4[i].w * kHRatio);
+            for (int64_t i = h->bnd_off[size_t(s)]; i < h->bnd_off[size_t(s) + 1]; ++i) mh[size_t(s)] = std::max(mh[size_t(s)], b4[i].w * kHRatio);
+        }
+        int r = build_layout(h, mh);
+        if (r) return r;
+        r = allocate(h);
+        if (r) return r;
+        h->bpos_user.resize(static_cast<size_t>(h->nb));
+        for (int64_t i = 0; i < h->nb; ++i) {
+            float4 b = b4[i];
+            b.w *= kHRatio;
+            h->bpos_user[size_t(i)] = b;
+        }
+        h->bvol_given = false;
+        h->have_boundary = true;
+        r = upload_boundary(h);
+        if (r) return r;
+    }
+    h->have_fluid = true;
+    return mps_set_fluid_f32(h, h->n, pos4, vel4, 0, stream);
+}
+
+int mps_get_batched(mps_handle* h, float* pos4, float* vel4, void* stream) {
+    return mps_get_fluid_f32(h, pos4, vel4, 0, stream);
+}
+
+int mps_get_scene_iters(mps_handle* h, int32_t* out3) {
+    const int r = check_ready(h);
+    if (r) return r;
+    DeviceGuard g(h->device);
+    MPS_CUDA_TRY(cudaDeviceSynchronize());
+    MPS_CUDA_TRY(cudaMemcpy(out3, h->scene_iters, 3 * size_t(h->nscenes) * sizeof(int), cudaMemcpyDeviceToHost));
+    return MPS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,226 @@
+// Internal declarations of the GB300 DFSPH step: device data layout, FP32 SPH kernel math,
+// launch wrappers.  Layout in HBM (all SoA, 16-byte aligned, "slot" = position in the
+// per-step cell-sorted order, scenes padded to a multiple of kPad slots so that every
+// thread block belongs to exactly one scene):
+//   pos4[slot]  = (x, y, z, h)      h = 4 r support radius, 0 for padding slots
+//   vel4[slot]  = (vx, vy, vz, m)
+//   ids[slot]   = particle ID given at set time
+//   nbr_f[k * slots + slot], nbr_b[k * slots + slot]  neighbour lists (interleaved so that a
+//                 warp reading its k-th neighbours touches one 128-byte line)
+//   cell tables: uint2 {start, end} per cell of each scene's grid (dense, validated against
+//                 slot_key so that stale entries need no clearing between steps)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mpsg {
+
+constexpr int kPad = 256;          // slot padding unit per scene
+constexpr int kChunk = 64;         // granularity of the slot -> scene table
+constexpr float kHRatio = 4.0f;    // support radius = 4 x particle radius
+
+// Per-scene constants.
+struct Scene {
+    float ox, oy, oz;               // grid origin
+    float cell, inv_cell;           // grid cell size (>= largest support radius) and 1/cell
+    int nx, ny, nz;                 // grid dims
+    unsigned long long key_base;    // first cell key of this scene
+    float bminx, bminy, bminz, bmaxx, bmaxy, bmaxz;   // collision box
+    int slot_begin, slot_end;       // padded fluid slots
+    int n;                          // real fluid particles (slots [slot_begin, slot_begin + n))
+    int coff;                       // compact offset (prefix of n over scenes)
+    int bbegin, bend;               // boundary particles of this scene (sorted order)
+};
+
+// Device-resident solver state of one scene.
+struct SceneSolve {
+    int active;       // still iterating
+    int do_update;    // run the second pass of this iteration
+    int iter;         // reference loop counter l
+    int blocks_done;  // blocks of this scene finished in the current pass
+    double err;       // last mean error (pressure) or r.r (CG)
+    double rr;        // CG: r.r of this iteration
+    double cg_alpha;  // CG step length
+    double cg_beta;   // CG direction update
+};
+
+struct StepCounters {
+    unsigned int scenes_done;   // scenes whose last block finished this pass
+    int nactive;                // scenes active at the start of the pass
+    int flags;                  // bit0 overflow, bit1 non-finite
+    int passes;                 // loop bodies run in the current solve (hard guard)
+    unsigned long long fluid_pairs, boundary_pairs;
+    unsigned long long iters_total[3];  // sum over steps and scenes of the loop counter (DF, CG, CD)
+    unsigned long long runs_total[3];   // loop bodies executed (the graph's WHILE iterations)
+};
+
+// Uniform parameters, passed by value to every kernel.
+struct Params {
+    float dt, inv_dt;
+    float gx, gy, gz;
+    float rho0, inv_rho0, V;      // rest density, particle volume
+    float visc, xsph, sigma;
+    float cg_factor;
+    int cubic;
+    int cap_f, cap_b;             // neighbour list capacities
+    int slots;                    // total padded slots
+    int nscenes;
+    int fixed_iters;
+    int min_iter_df, min_iter_cd, max_iter, cg_max_iter;
+    float df_tol, cd_tol, cg_tol; // stored as float for the kernel args; compared in FP64
+    double df_tol_d, cd_tol_d, cg_tol_d;
+};
+
+// Device pointers of one step (buffer a is read, buffer b written by the reorder).
+struct Dev {
+    float4 *pos, *vel;            // current (sorted) state
+    unsigned int* ids;
+    float4 *pos_in, *vel_in;      // previous order (reorder source)
+    unsigned int* ids_in;
+    unsigned long long* slot_key;
+    uint2* ftable;                // fluid cell table
+    uint2* btable;                // boundary cell table
+    const Scene* scenes;
+    const int* chunk_scene;       // slot/kChunk -> scene
+    unsigned int* nbr_f;
+    unsigned int* nbr_b;
+    unsigned int* cnt;            // nf | nb << 16
+    float* rho;
+    float* alpha;
+    float* kappa;
+    float* delta;
+    float2* aux;                  // (rho, st factor) packed for the CG gathers
+    float4* color;
+    float4 *cg_x, *cg_r, *cg_p, *cg_ap, *cg_b;
+    const float4* bpos;           // boundary (x, y, z, h)
+    float* bvol;
+    double* partial;              // per-block FP64 partial sums (2 per block)
+    SceneSolve* solve;
+    StepCounters* ctr;
+    int* scene_iters;             // 3 per scene (DF, CG, CD) of the last step
+    double* scene_err;            // 3 per scene
+    unsigned long long* keys;     // compact keys (sorted in place by the radix sort)
+    unsigned int* vals;
+};
+
+// ------------------------------------------------------------------ FP32 kernel math
+// Constants of MPSSPHKernel.cuh:9-14 written from their formulas.
+#define MPSG_PI_F 3.14159265358979323846f
+struct KC {
+    static constexpr float w = 315.0f / (64.0f * MPSG_PI_F);
+    static constexpr float g = 45.0f / MPSG_PI_F;
+    static constexpr float cw = 8.0f / MPSG_PI_F;
+    static constexpr float cg = 48.0f / MPSG_PI_F;
+    static constexpr float stw = 8.0f / MPSG_PI_F * 10.0f / 7.0f * 2.0f;
+    static constexpr float stg = 48.0f / MPSG_PI_F * 10.0f / 7.0f;
+};
+
+// W(d) with q = d / h (poly6 or cubic spline), MPSSPHKernel.cuh:28-45.
+__device__ __forceinline__ float kW(float d, float invh, int cubic) {
+    const float q = d * invh;
+    if (q >= 1.0f) return 0.0f;
+    if (cubic) {
+        if (q >= 0.5f) {
+            const float t = (1.0f - q) * invh;
+            return KC::cw * 2.0f * t * t * t;
+        }
+        return KC::cw * invh * invh * invh * ((6.0f * q - 6.0f) * q * q + 1.0f);
+    }
+    const float t = (1.0f - q * q) * invh;
+    return KC::w * t * t * t;
+}
+// G(d) with grad W = G x_ij, MPSSPHKernel.cuh:46-65.  invd = 1/d.
+__device__ __forceinline__ float kG(float d, float invd, float invh, int cubic) {
+    const float q = d * invh;
+    if (q < 1.0e-20f || q >= 1.0f) return 0.0f;
+    const float invh2 = invh * invh;
+    if (cubic) {
+        if (q > 0.5f) {
+            const float t = (1.0f - q) * invh2;
+            return -KC::cg * invd * t * t;
+        }
+        return KC::cg * invd * invh2 * invh2 * (3.0f * q - 2.0f) * q;
+    }
+    const float t = (1.0f - q) * invh2;
+    return -KC::g * invd * t * t;
+}
+// Surface-tension kernels, MPSSPHKernel.cuh:67-84.
+__device__ __forceinline__ float kSTW(float d, float invh) {
+    const float q = fmaxf(d * invh, 0.5f);
+    if (q >= 1.0f) return 0.0f;
+    const float t = (1.0f - q) * invh;
+    return KC::stw * t * t * t;
+}
+__device__ __forceinline__ float kSTG(float d, float invd, float invh) {
+    const float q = d * invh;
+    if (q <= 0.5f || q >= 1.0f) return 0.0f;
+    const float t = (1.0f - q) * invh * invh;
+    return -KC::stg * invd * t * t;
+}
+
+// Squared distance with an explicit operation order (no implicit contraction), shared with
+// the oracle's FP32 neighbour test: fma(dz,dz,fma(dy,dy,dx*dx)).
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// 1/d for a pair; 0 for coincident particles so that d = d2 * (1/d) = 0 and G(0) = 0.
+__device__ __forceinline__ float safe_rsqrt(float d2) { return d2 > 0.0f ? rsqrtf(d2) : 0.0f; }
+
+// Kahan-compensated FP32 accumulator.
+struct Kahan {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = __fsub_rn(x, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+
+__device__ __forceinline__ int cell_coord(float x, float o, float inv, int dim) {
+    const float t = __fmul_rn(__fsub_rn(x, o), inv);
+    if (!(t >= 0.0f)) return 0;
+    if (t >= float(dim)) return dim - 1;
+    const int c = int(t);
+    return c < dim ? c : dim - 1;
+}
+
+// ------------------------------------------------------------------ launch wrappers
+// Radix sort of (key, val) pairs by the low `bits` bits of key; stable.  Uses tmp buffers of
+// the same size; the result ends in keys/vals.  Returns cudaError_t.
+cudaError_t radix_sort_pairs(unsigned long long* keys, unsigned int* vals,
+                             unsigned long long* keys_tmp, unsigned int* vals_tmp,
+                             unsigned int* counts, int n, int bits, int digit_bits,
+                             cudaStream_t s);
+size_t radix_counts_size(int n);
+
+void launch_keys(const Dev& d, const Params& p, cudaStream_t s);
+void launch_reorder(const Dev& d, const Params& p, int n_real, cudaStream_t s);
+void launch_build_nbrs(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_bvolume(const Dev& d, const Params& p, int nb, int accumulate, cudaStream_t s);
+void launch_density_alpha(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_solver_init(const Dev& d, const Params& p, cudaStream_t s);
+void launch_set_cond(const Dev& d, unsigned long long cond, cudaStream_t s);
+void launch_load_state(const Dev& d, const Params& p, const float4* pos4, const float4* vel4, int n,
+                       cudaStream_t s);
+void launch_store_state(const Dev& d, const Params& p, float4* pos4, float4* vel4, cudaStream_t s);
+void launch_pressure_A(const Dev& d, const Params& p, int mode, int bs,
+                       unsigned long long cond, int use_cond, cudaStream_t s);
+void launch_pressure_B(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                       cudaStream_t s);
+void launch_pressure_B_profile(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_solver_finish(const Dev& d, const Params& p, int which, cudaStream_t s);
+void launch_st_factor(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_cg_ax0(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond,
+                  cudaStream_t s);
+void launch_cg_update(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_cg_dir(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                   cudaStream_t s);
+void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);
+void launch_advect(const Dev& d, const Params& p, cudaStream_t s);
+void launch_stats(const Dev& d, const Params& p, cudaStream_t s);
+
+}  // namespace mpsg

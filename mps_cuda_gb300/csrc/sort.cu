@@ -1,0 +1,166 @@
+// Stable LSD radix sort of (64-bit cell key, 32-bit slot) pairs over the significant key bits
+// only.  Replaces the thrust::sort_by_key of SpatialHash::UpdateHash (MPSSpatialHash.cu:69),
+// whose stability fixes the within-cell order; this sort keeps the same stability guarantee.
+//
+// One pass per digit (digit_bits <= 8):
+//   upsweep  : per-tile digit histogram (warp-aggregated shared atomics), digit-major counts
+//   scan     : exclusive scan of the digit-major counts (one block)
+//   downsweep: per-warp stable ranks with __match_any_sync, cross-warp prefix per digit, scatter
+// Tiles are 8 warps x 32 lanes x 16 items; each warp owns a contiguous run of 512 keys, so
+// (warp, round, lane) order equals input order and the scatter is stable.
+#include "mps_internal.cuh"
+
+namespace mpsg {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kIpt = 16;
+constexpr int kTile = kThreads * kIpt;
+constexpr int kBins = 256;
+constexpr int kScanThreads = 1024;
+
+__global__ void __launch_bounds__(kThreads) rs_upsweep(const unsigned long long* __restrict__ keys, int n,
+                                                       int shift, unsigned int mask, int nblocks,
+                                                       unsigned int* __restrict__ counts) {
+    __shared__ unsigned int hist[kBins];
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wbase = blockIdx.x * kTile + warp * 32 * kIpt;
+#pragma unroll 4
+    for (int r = 0; r < kIpt; ++r) {
+        const int idx = wbase + r * 32 + lane;
+        const bool valid = idx < n;
+        const unsigned int d = valid ? unsigned((keys[idx] >> shift) & mask) : 0xffffffffu;
+        const unsigned int peers = __match_any_sync(0xffffffffu, d);
+        if (valid && lane == __ffs(peers) - 1) atomicAdd(&hist[d], unsigned(__popc(peers)));
+    }
+    __syncthreads();
+    counts[threadIdx.x * nblocks + blockIdx.x] = hist[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kScanThreads) rs_scan(unsigned int* __restrict__ counts, int total) {
+    __shared__ unsigned int warp_sums[kScanThreads / 32];
+    const int chunk = (total + kScanThreads - 1) / kScanThreads;
+    const int begin = threadIdx.x * chunk;
+    const int end = min(begin + chunk, total);
+    unsigned int sum = 0;
+    for (int i = begin; i < end; ++i) sum += counts[i];
+    // block exclusive scan of per-thread sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned int w = warp_sums[lane];
+        unsigned int wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int v = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += v;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    unsigned int run = warp_sums[warp] + incl - sum;
+    for (int i = begin; i < end; ++i) {
+        const unsigned int c = counts[i];
+        counts[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) rs_downsweep(const unsigned long long* __restrict__ kin,
+                                                         const unsigned int* __restrict__ vin,
+                                                         unsigned long long* __restrict__ kout,
+                                                         unsigned int* __restrict__ vout, int n,
+                                                         int shift, unsigned int mask, int nblocks,
+                                                         const unsigned int* __restrict__ offsets) {
+    __shared__ unsigned int wcnt[kWarps][kBins];
+    __shared__ unsigned int s_off[kBins];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) wcnt[w][threadIdx.x] = 0;
+    s_off[threadIdx.x] = offsets[threadIdx.x * nblocks + blockIdx.x];
+    __syncthreads();
+    const int wbase = blockIdx.x * kTile + warp * 32 * kIpt;
+    const unsigned int lt = (1u << lane) - 1u;
+    unsigned long long k[kIpt];
+    unsigned int v[kIpt];
+    unsigned int rank[kIpt];
+#pragma unroll
+    for (int r = 0; r < kIpt; ++r) {
+        const int idx = wbase + r * 32 + lane;
+        const bool valid = idx < n;
+        k[r] = valid ? kin[idx] : 0ull;
+        v[r] = valid ? vin[idx] : 0u;
+        const unsigned int d = valid ? unsigned((k[r] >> shift) & mask) : 0xffffffffu;
+        const unsigned int peers = __match_any_sync(0xffffffffu, d);
+        const unsigned int base = valid ? wcnt[warp][d] : 0u;
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = base + unsigned(__popc(peers));
+        __syncwarp();
+        rank[r] = base + unsigned(__popc(peers & lt));
+    }
+    __syncthreads();
+    {   // exclusive prefix over warps for digit threadIdx.x
+        unsigned int run = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const unsigned int c = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kIpt; ++r) {
+        const int idx = wbase + r * 32 + lane;
+        if (idx < n) {
+            const unsigned int d = unsigned((k[r] >> shift) & mask);
+            const unsigned int dst = s_off[d] + wcnt[warp][d] + rank[r];
+            kout[dst] = k[r];
+            vout[dst] = v[r];
+        }
+    }
+}
+}  // namespace
+
+size_t radix_counts_size(int n) {
+    const int nblocks = (n + kTile - 1) / kTile;
+    return size_t(kBins) * size_t(nblocks > 0 ? nblocks : 1);
+}
+
+cudaError_t radix_sort_pairs(unsigned long long* keys, unsigned int* vals, unsigned long long* keys_tmp,
+                             unsigned int* vals_tmp, unsigned int* counts, int n, int bits, int digit_bits,
+                             cudaStream_t s) {
+    if (n <= 1 || bits <= 0) return cudaSuccess;
+    if (digit_bits < 1 || digit_bits > 8) digit_bits = 8;
+    const int nblocks = (n + kTile - 1) / kTile;
+    const int passes = (bits + digit_bits - 1) / digit_bits;
+    unsigned long long *ka = keys, *kb = keys_tmp;
+    unsigned int *va = vals, *vb = vals_tmp;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = p * digit_bits;
+        const int nb = min(digit_bits, bits - shift);
+        const unsigned int mask = (1u << nb) - 1u;
+        rs_upsweep<<<nblocks, kThreads, 0, s>>>(ka, n, shift, mask, nblocks, counts);
+        rs_scan<<<1, kScanThreads, 0, s>>>(counts, kBins * nblocks);
+        rs_downsweep<<<nblocks, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, mask, nblocks, counts);
+        unsigned long long* tk = ka; ka = kb; kb = tk;
+        unsigned int* tv = va; va = vb; vb = tv;
+    }
+    if (ka != keys) {
+        cudaMemcpyAsync(keys, ka, size_t(n) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(vals, va, size_t(n) * sizeof(unsigned int), cudaMemcpyDeviceToDevice, s);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mpsg

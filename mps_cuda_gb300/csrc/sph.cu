@@ -1,0 +1,829 @@
+// SPH kernels of the GB300 DFSPH step.  One thread per slot (cell-sorted particle).
+// Reference counterparts (moonsh5009/MPS_CUDA):
+//   k_keys / k_reorder     SpatialHash::UpdateHash, InitHash_kernel, ReorderHash_kernel
+//                          (src/MPS_Object/MPSSpatialHash.cu:53-77, .cuh:83-145); new scheme:
+//                          clamped floor cells, 64-bit keys, stable radix sort, SoA reorder.
+//   k_build_nbrs           BuildNeighorhood x3 (MPSSpatialHash.cu:142-218, .cuh:147-271);
+//                          one pass over 9 cell rows instead of count+scan+fill.
+//   k_bvolume              ComputeBoundaryParticleVolume* (MPSSPHBaseUtil.cuh:10-86)
+//   k_density_alpha        ComputeDensity*, DensityColorTest, ComputeDFSPHFactor*, ResetForce,
+//                          ApplyGravity, UpdateVelocity (MPSSystem.cpp:240-255) fused.
+//   k_pressure_A / _B      ComputeDensityDelta* + Compute{DF,CD}Stiffness + residual
+//                          (MPSSPHDFSPHUtil.cuh:139-340) / ApplyDFSPH* + UpdateVelocity
+//                          (:342-468); loop control of MPSSPHDFSPHUtil.cu:270-441 on the device.
+//   k_st_factor, k_cg_*    ComputeSurfaceTensionFactor/CGb/CGAp, ComputeCGViscosityAp,
+//                          ComputeFinalCGAp (MPSSPHNonPressureUtil.cuh:425-648) and CGSolver
+//                          (MPSSolver.cuh:12-73, MPSCGKernel.cuh:5-133) with device-side dots.
+//   k_advect               BoundaryCollision + UpdatePosition (MPSAdvectUtil.cuh:36-77).
+#include "mps_internal.cuh"
+
+namespace mpsg {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kFltEps = 1.1920928955078125e-07f;
+
+__device__ __forceinline__ int block_scene(const Dev& d, int bs) {
+    return d.chunk_scene[(blockIdx.x * bs) / kChunk];
+}
+
+template <int BS>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < BS / 32 ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+        if (lane == 0) sh[0] = v;
+    }
+    __syncthreads();
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// Deterministic sum of this scene's per-block partials (component c of 2), run by one block.
+template <int BS>
+__device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double* sh) {
+    const int b0 = sc.slot_begin / BS, b1 = sc.slot_end / BS;
+    double v = 0.0;
+    for (int b = b0 + threadIdx.x; b < b1; b += BS) v += __ldcg(d.partial + 2 * b + c);
+    return block_sum<BS>(v, sh);
+}
+
+// Returns true in every thread of the block that is the last of its scene to finish.
+template <int BS>
+__device__ bool last_block_of_scene(const Dev& d, int s, const Scene& sc) {
+    __shared__ int am_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned nblk = unsigned((sc.slot_end - sc.slot_begin) / BS);
+        const unsigned t = atomicAdd(reinterpret_cast<unsigned*>(&d.solve[s].blocks_done), 1u);
+        am_last = (t == nblk - 1u);
+        if (am_last) d.solve[s].blocks_done = 0;
+    }
+    __syncthreads();
+    return am_last != 0;
+}
+
+// Called by thread 0 of the last block of each active scene after its decision: the last
+// scene to decide counts the scenes still active and sets the loop condition.
+__device__ void finish_scene_decision(const Dev& d, const Params& p, unsigned long long cond, int use_cond) {
+    __threadfence();
+    const unsigned t = atomicAdd(&d.ctr->scenes_done, 1u);
+    const int nact = *reinterpret_cast<volatile int*>(&d.ctr->nactive);
+    if (t == unsigned(nact) - 1u) {
+        __threadfence();
+        int cnt = 0;
+        for (int s = 0; s < p.nscenes; ++s) cnt += *reinterpret_cast<volatile int*>(&d.solve[s].active);
+        d.ctr->nactive = cnt;
+        d.ctr->scenes_done = 0;
+        if (use_cond) cudaGraphSetConditional(cond, cnt > 0 ? 1u : 0u);
+    }
+}
+
+// Run by one thread in the last kernel of a loop body: counts the bodies of this solve and ends
+// the loop (flag bit 2) if it ran past its limit, whatever the per-scene decisions said.
+__device__ void loop_guard(const Dev& d, unsigned long long cond, int limit) {
+    const int passes = atomicAdd(&d.ctr->passes, 1) + 1;
+    if (passes >= limit) {
+        atomicOr(&d.ctr->flags, 4);
+        cudaGraphSetConditional(cond, 0u);
+    }
+}
+
+// ------------------------------------------------------------------ sort / reorder
+__global__ void k_keys(Dev d, Params p) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= p.slots) return;
+    const Scene& sc = d.scenes[d.chunk_scene[slot / kChunk]];
+    if (slot >= sc.slot_begin + sc.n) return;
+    const float4 x = d.pos_in[slot];
+    if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(&d.ctr->flags, 2);
+    const int cx = cell_coord(x.x, sc.ox, sc.inv_cell, sc.nx);
+    const int cy = cell_coord(x.y, sc.oy, sc.inv_cell, sc.ny);
+    const int cz = cell_coord(x.z, sc.oz, sc.inv_cell, sc.nz);
+    const int k = sc.coff + (slot - sc.slot_begin);
+    d.keys[k] = sc.key_base + (static_cast<unsigned long long>(cz) * unsigned(sc.ny) + unsigned(cy)) * unsigned(sc.nx) + unsigned(cx);
+    d.vals[k] = unsigned(slot);
+}
+
+__global__ void k_reorder(Dev d, Params p, int n_real) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_real) return;
+    const unsigned long long key = d.keys[k];
+    const unsigned src = d.vals[k];
+    int lo = 0, hi = p.nscenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.scenes[mid].coff <= k) lo = mid; else hi = mid - 1;
+    }
+    const Scene& sc = d.scenes[lo];
+    const unsigned dst = unsigned(sc.slot_begin + (k - sc.coff));
+    d.pos[dst] = d.pos_in[src];
+    d.vel[dst] = d.vel_in[src];
+    d.ids[dst] = d.ids_in[src];
+    d.slot_key[dst] = key;
+    if (k == 0 || d.keys[k - 1] != key) d.ftable[key].x = dst;
+    if (k == n_real - 1 || d.keys[k + 1] != key) d.ftable[key].y = dst + 1u;
+}
+
+// Fluid cell lookup; stale entries of cells emptied since an earlier step fail the key check.
+__device__ __forceinline__ bool fluid_cell(const Dev& d, int slots, unsigned long long key, uint2& e) {
+    e = d.ftable[key];
+    return e.x < e.y && e.x < unsigned(slots) && d.slot_key[e.x] == key;
+}
+
+// ------------------------------------------------------------------ neighbour lists
+template <int BS>
+__global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const Scene& sc = d.scenes[block_scene(d, BS)];
+    __shared__ unsigned long long s_pf, s_pb;
+    if (threadIdx.x == 0) { s_pf = 0; s_pb = 0; }
+    __syncthreads();
+    unsigned nf = 0, nb = 0;
+    if (i < sc.slot_begin + sc.n) {
+        const float4 xi = d.pos[i];
+        const int cx = cell_coord(xi.x, sc.ox, sc.inv_cell, sc.nx);
+        const int cy = cell_coord(xi.y, sc.oy, sc.inv_cell, sc.ny);
+        const int cz = cell_coord(xi.z, sc.oz, sc.inv_cell, sc.nz);
+        const int x0 = max(cx - 1, 0), x1 = min(cx + 1, sc.nx - 1);
+        const size_t stride = size_t(p.slots);
+        bool over = false;
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int z = cz + dz;
+            if (z < 0 || z >= sc.nz) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = cy + dy;
+                if (y < 0 || y >= sc.ny) continue;
+                const unsigned long long row = sc.key_base + (static_cast<unsigned long long>(z) * unsigned(sc.ny) + unsigned(y)) * unsigned(sc.nx);
+                unsigned fb = 0xffffffffu, fe = 0u, bb = 0xffffffffu, be = 0u;
+                for (int x = x0; x <= x1; ++x) {
+                    uint2 e;
+                    if (fluid_cell(d, p.slots, row + unsigned(x), e)) { fb = min(fb, e.x); fe = max(fe, e.y); }
+                    const uint2 eb = d.btable[row + unsigned(x)];
+                    if (eb.x < eb.y) { bb = min(bb, eb.x); be = max(be, eb.y); }
+                }
+                for (unsigned j = fb; j < fe; ++j) {
+                    if (j == unsigned(i)) continue;
+                    const float4 xj = d.pos[j];
+                    const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
+                    const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
+                    if (d2 < __fmul_rn(hij, hij)) {
+                        if (nf < unsigned(p.cap_f)) d.nbr_f[size_t(nf) * stride + size_t(i)] = j; else over = true;
+                        nf++;
+                    }
+                }
+                for (unsigned j = bb; j < be; ++j) {
+                    const float4 xj = d.bpos[j];
+                    const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
+                    const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
+                    if (d2 < __fmul_rn(hij, hij)) {
+                        if (nb < unsigned(p.cap_b)) d.nbr_b[size_t(nb) * stride + size_t(i)] = j; else over = true;
+                        nb++;
+                    }
+                }
+            }
+        }
+        if (over) atomicOr(&d.ctr->flags, 1);
+        nf = min(nf, unsigned(p.cap_f));
+        nb = min(nb, unsigned(p.cap_b));
+        atomicAdd(&s_pf, (unsigned long long)nf);
+        atomicAdd(&s_pb, (unsigned long long)nb);
+    }
+    d.cnt[i] = nf | (nb << 16);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(&d.ctr->fluid_pairs, s_pf);
+        atomicAdd(&d.ctr->boundary_pairs, s_pb);
+    }
+}
+
+// ------------------------------------------------------------------ boundary volume
+// V_b = 1 / (prev + W(0) + sum_k W(|x_b - x_k|)) over boundary neighbours (Akinci).
+__global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    int lo = 0, hi = p.nscenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.scenes[mid].bbegin <= b) lo = mid; else hi = mid - 1;
+    }
+    const Scene& sc = d.scenes[lo];
+    const float4 xi = d.bpos[b];
+    const float invh = 1.0f / xi.w;
+    const int cx = cell_coord(xi.x, sc.ox, sc.inv_cell, sc.nx);
+    const int cy = cell_coord(xi.y, sc.oy, sc.inv_cell, sc.ny);
+    const int cz = cell_coord(xi.z, sc.oz, sc.inv_cell, sc.nz);
+    Kahan sum;
+    sum.add(kW(0.0f, invh, p.cubic));
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, sc.nz - 1); ++z)
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, sc.ny - 1); ++y)
+            for (int x = max(cx - 1, 0); x <= min(cx + 1, sc.nx - 1); ++x) {
+                const uint2 e = d.btable[sc.key_base + (static_cast<unsigned long long>(z) * unsigned(sc.ny) + unsigned(y)) * unsigned(sc.nx) + unsigned(x)];
+                for (unsigned j = e.x; j < e.y; ++j) {
+                    if (j == unsigned(b)) continue;
+                    const float4 xj = d.bpos[j];
+                    const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+                    const float d2 = dist2(dx, dy, dz);
+                    const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
+                    if (d2 < __fmul_rn(hij, hij)) sum.add(kW(sqrtf(d2), invh, p.cubic));
+                }
+            }
+    const float prev = accumulate ? d.bvol[b] : 0.0f;
+    d.bvol[b] = 1.0f / (prev + sum.s);
+}
+
+// ------------------------------------------------------------------ density + alpha + gravity
+template <int BS>
+__global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const Scene& sc = d.scenes[block_scene(d, BS)];
+    if (i >= sc.slot_begin + sc.n) return;
+    const size_t stride = size_t(p.slots);
+    const float4 xi = d.pos[i];
+    const float invh = 1.0f / xi.w;
+    const unsigned c = d.cnt[i];
+    const int nf = int(c & 0xffffu), nb = int(c >> 16);
+    Kahan rf, gx, gy, gz, sq;
+    rf.add(p.V * kW(0.0f, invh, p.cubic));
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+        const float4 xj = d.pos[j];
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float dist = d2 * invd;
+        rf.add(p.V * kW(dist, invh, p.cubic));
+        const float g = p.V * kG(dist, invd, invh, p.cubic);
+        const float ax = g * dx, ay = g * dy, az = g * dz;
+        gx.add(ax); gy.add(ay); gz.add(az);
+        sq.add(ax * ax + ay * ay + az * az);
+    }
+    Kahan rb;
+    for (int k = 0; k < nb; ++k) {
+        const unsigned j = d.nbr_b[size_t(k) * stride + size_t(i)];
+        const float4 xj = d.bpos[j];
+        const float vb = d.bvol[j];
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float dist = d2 * invd;
+        rb.add(vb * kW(dist, invh, p.cubic));
+        const float g = vb * kG(dist, invd, invh, p.cubic);
+        gx.add(g * dx); gy.add(g * dy); gz.add(g * dz);
+    }
+    const float rho = (rf.s + rb.s) * p.rho0;
+    d.rho[i] = rho;
+    // alpha denominator in FP64: |sum grad|^2 + sum |grad|^2, clamp at 1e-20 (MPSSPHDFSPHUtil.cuh:127-137)
+    const double sx = gx.s, sy = gy.s, sz = gz.s;
+    const double f = double(sq.s) + (sx * sx + sy * sy + sz * sz);
+    d.alpha[i] = f > 1.0e-20 ? float(1.0 / f) : 0.0f;
+    const float ratio = rho * p.inv_rho0;
+    float4 col;
+    col.x = fminf(fmaxf(ratio - 1.0f, 0.0f), 1.0f);
+    col.y = fminf(fmaxf(ratio < 1.0f ? ratio : 1.0f - (ratio - 1.0f), 0.0f), 1.0f);
+    col.z = fminf(fmaxf(1.0f - ratio, 0.0f), 1.0f);
+    col.w = 1.0f;
+    d.color[i] = col;
+    float4 v = d.vel[i];
+    if (v.w > 1.0e-10f) { v.x += p.dt * p.gx; v.y += p.dt * p.gy; v.z += p.dt * p.gz; }
+    d.vel[i] = v;
+}
+
+// ------------------------------------------------------------------ pressure solves
+__global__ void k_solver_init(Dev d, Params p) {
+    __shared__ int cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < p.nscenes; s += blockDim.x) {
+        SceneSolve& S = d.solve[s];
+        S.active = d.scenes[s].n > 0 ? 1 : 0;
+        S.do_update = 0;
+        S.iter = 1;
+        S.blocks_done = 0;
+        S.err = 0.0;
+        S.rr = 0.0;
+        S.cg_alpha = 0.0;
+        S.cg_beta = 0.0;
+        if (S.active) atomicAdd(&cnt, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        d.ctr->nactive = cnt;
+        d.ctr->scenes_done = 0;
+        d.ctr->passes = 0;
+    }
+}
+
+__global__ void k_set_cond(Dev d, unsigned long long cond) {
+    cudaGraphSetConditional(cond, d.ctr->nactive > 0 ? 1u : 0u);
+}
+
+// Pass A: density change rate delta, stiffness kappa, mean-error reduction and loop decision.
+// mode 0: divergence-free, kappa = min(dt delta, rho/rho0 + dt delta - 0.8);
+// mode 1: constant density, kappa = rho/rho0 + dt delta - 1 (MPSSPHDFSPHUtil.cuh:259-340).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, unsigned long long cond, int use_cond) {
+    __shared__ double sh[32];
+    const int s = block_scene(d, BS);
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    float err = 0.0f;
+    if (i < sc.slot_begin + sc.n) {
+        const size_t stride = size_t(p.slots);
+        const float4 xi = d.pos[i];
+        const float4 vi = d.vel[i];
+        const float invh = 1.0f / xi.w;
+        const unsigned c = d.cnt[i];
+        const int nf = int(c & 0xffffu), nb = int(c >> 16);
+        float df = 0.0f;
+        for (int k = 0; k < nf; ++k) {
+            const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+            const float4 xj = d.pos[j];
+            const float4 vj = d.vel[j];
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float invd = safe_rsqrt(d2);
+            const float g = kG(d2 * invd, invd, invh, p.cubic);
+            df += g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
+        }
+        float db = 0.0f;
+        for (int k = 0; k < nb; ++k) {
+            const unsigned j = d.nbr_b[size_t(k) * stride + size_t(i)];
+            const float4 xj = d.bpos[j];
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float invd = safe_rsqrt(d2);
+            const float g = kG(d2 * invd, invd, invh, p.cubic);
+            db += d.bvol[j] * g * (dx * vi.x + dy * vi.y + dz * vi.z);
+        }
+        const float delta = p.V * df + db;
+        const float r = d.rho[i] * p.inv_rho0;
+        float kap = mode == 0 ? fminf(delta * p.dt, r + p.dt * delta - 0.8f) : r + p.dt * delta - 1.0f;
+        if (kap > 0.0f) {
+            err = kap;
+            kap *= d.alpha[i] * (p.inv_dt * p.inv_dt);
+        } else {
+            kap = 0.0f;
+        }
+        d.kappa[i] = kap;
+        d.delta[i] = delta;
+    }
+    const double bsum = block_sum<BS>(double(err), sh);
+    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bsum;
+    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
+    const double tot = scene_partial_sum<BS>(d, sc, 0, sh);
+    if (threadIdx.x == 0) {
+        SceneSolve& S = d.solve[s];
+        const double mean = tot / double(sc.n);
+        const int l = S.iter;
+        const double tol = mode == 0 ? p.df_tol_d : p.cd_tol_d;
+        const int minl = mode == 0 ? p.min_iter_df : p.min_iter_cd;
+        const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.max_iter;
+        const bool stop = p.fixed_iters > 0 ? false : (mean < tol && l > minl);
+        S.err = mean;
+        if (stop) {
+            S.active = 0;
+            S.do_update = 0;
+        } else {
+            S.do_update = 1;
+            S.iter = l + 1;
+            if (l + 1 > cap) S.active = 0;
+        }
+        finish_scene_decision(d, p, cond, use_cond);
+    }
+}
+
+// Pass B: pressure force and velocity update, v += dt * F (ApplyDFSPH* + Final + UpdateVelocity).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile, unsigned long long cond, int use_cond, int limit) {
+    if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int s = block_scene(d, BS);
+    if (!profile && !d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    if (i >= sc.slot_begin + sc.n) return;
+    const size_t stride = size_t(p.slots);
+    const float4 xi = d.pos[i];
+    const float invh = 1.0f / xi.w;
+    const float ki = d.kappa[i];
+    const unsigned c = d.cnt[i];
+    const int nf = int(c & 0xffffu), nb = int(c >> 16);
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+        const float4 xj = d.pos[j];
+        const float kj = d.kappa[j];
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float g = (ki + kj) * kG(d2 * invd, invd, invh, p.cubic);
+        fx -= g * dx; fy -= g * dy; fz -= g * dz;
+    }
+    fx *= 0.5f * p.V; fy *= 0.5f * p.V; fz *= 0.5f * p.V;
+    if (ki != 0.0f) {
+        float bx = 0.0f, by = 0.0f, bz = 0.0f;
+        for (int k = 0; k < nb; ++k) {
+            const unsigned j = d.nbr_b[size_t(k) * stride + size_t(i)];
+            const float4 xj = d.bpos[j];
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float invd = safe_rsqrt(d2);
+            const float g = d.bvol[j] * kG(d2 * invd, invd, invh, p.cubic);
+            bx -= g * dx; by -= g * dy; bz -= g * dz;
+        }
+        const float h = 0.5f * ki;
+        fx += h * bx; fy += h * by; fz += h * bz;
+    }
+    float4 v = d.vel[i];
+    if (v.w > 1.0e-10f) { v.x += p.dt * fx; v.y += p.dt * fy; v.z += p.dt * fz; }
+    d.vel[i] = v;
+}
+
+// Records the loop counter and error of solve `which` (0 DF, 1 CG, 2 CD) per scene.
+// Also accumulates the loop counters and the number of loop bodies run (max over scenes).
+__global__ void k_solver_finish(Dev d, Params p, int which) {
+    __shared__ unsigned long long sum;
+    __shared__ int runs;
+    if (threadIdx.x == 0) { sum = 0; runs = 0; }
+    __syncthreads();
+    const int cap = p.fixed_iters > 0 ? p.fixed_iters : (which == 1 ? p.cg_max_iter : p.max_iter);
+    for (int s = threadIdx.x; s < p.nscenes; s += blockDim.x) {
+        const int it = d.solve[s].iter;
+        d.scene_iters[3 * s + which] = it;
+        d.scene_err[3 * s + which] = d.solve[s].err;
+        if (d.scenes[s].n > 0) {
+            atomicAdd(&sum, (unsigned long long)it);
+            atomicMax(&runs, min(it, cap));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        d.ctr->iters_total[which] += sum;
+        d.ctr->runs_total[which] += (unsigned long long)runs;
+    }
+}
+
+// ------------------------------------------------------------------ viscosity + surface tension
+template <int BS>
+__global__ void __launch_bounds__(BS) k_st_factor(Dev d, Params p) {
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const Scene& sc = d.scenes[block_scene(d, BS)];
+    if (i >= sc.slot_begin + sc.n) return;
+    const size_t stride = size_t(p.slots);
+    const float4 xi = d.pos[i];
+    const float4 vi = d.vel[i];
+    const float invh = 1.0f / xi.w;
+    const int nf = int(d.cnt[i] & 0xffffu);
+    float acc = 0.0f;
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+        const float4 xj = d.pos[j];
+        const float4 vj = d.vel[j];
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float g = kG(d2 * invd, invd, invh, p.cubic);
+        acc += vj.w * g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
+    }
+    d.aux[i] = make_float2(d.rho[i], acc);
+}
+
+// g_ij of the surface-tension operator (MPSSPHNonPressureUtil.cuh:510-515).
+struct StPair {
+    float gij, w, G, dist;
+};
+
+// b_i = v_i + dt sigma / m_i sum_j -mbar_ij g_ij x_ij; x0 = v (MPSSPHNonPressureUtil.cuh:467-521).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const Scene& sc = d.scenes[block_scene(d, BS)];
+    if (i >= sc.slot_begin + sc.n) return;
+    const size_t stride = size_t(p.slots);
+    const float4 xi = d.pos[i];
+    const float4 vi = d.vel[i];
+    const float2 ai = d.aux[i];
+    const float invh = 1.0f / xi.w;
+    const int nf = int(d.cnt[i] & 0xffffu);
+    float bx = 0.0f, by = 0.0f, bz = 0.0f;
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+        const float4 xj = d.pos[j];
+        const float4 vj = d.vel[j];
+        const float2 aj = d.aux[j];
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float dist = d2 * invd;
+        const float invD = 2.0f / (ai.x + aj.x);
+        const float stw = kSTW(dist, invh);
+        const float stg = kSTG(dist, invd, invh);
+        const float vdot = stg * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
+        const float gij = (stw + p.dt * (vdot - (ai.y + aj.y) * invD * 0.5f * stw)) * invD;
+        const float c = 0.5f * (vi.w + vj.w) * gij;
+        bx -= c * dx; by -= c * dy; bz -= c * dz;
+    }
+    const float sc_ = p.dt * p.sigma / vi.w;
+    d.cg_b[i] = make_float4(vi.x + sc_ * bx, vi.y + sc_ * by, vi.z + sc_ * bz, 0.0f);
+    d.cg_x[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
+}
+
+// (A q)_i = q_i (1 + f) + dt (ST + XSPH + viscosity) (MPSSPHNonPressureUtil.cuh:523-648).
+__device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, const float4* q, float factor) {
+    const size_t stride = size_t(p.slots);
+    const float4 xi = d.pos[i];
+    const float4 vi = d.vel[i];
+    const float2 ai = d.aux[i];
+    const float4 qi = q[i];
+    const float hi = xi.w;
+    const float invh = 1.0f / hi;
+    const float eps_h2 = 0.01f * hi * hi;
+    const int nf = int(d.cnt[i] & 0xffffu);
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;   // surface tension + XSPH, already scaled per pair
+    float vx = 0.0f, vy = 0.0f, vz = 0.0f;   // viscosity
+    const float st_scale = p.dt * p.sigma / vi.w;
+    const float xs_scale = p.xsph * p.inv_dt;
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+        const float4 xj = d.pos[j];
+        const float4 vj = d.vel[j];
+        const float2 aj = d.aux[j];
+        const float4 qj = q[j];
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float dist = d2 * invd;
+        const float invD = 2.0f / (ai.x + aj.x);
+        const float stw = kSTW(dist, invh);
+        const float stg = kSTG(dist, invd, invh);
+        const float vdot = stg * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
+        const float gij = (stw + p.dt * (vdot - (ai.y + aj.y) * invD * 0.5f * stw)) * invD;
+        const float w = kW(dist, invh, p.cubic);
+        const float c = st_scale * 0.5f * (vi.w + vj.w) * gij + xs_scale * (vj.w / aj.x) * w;
+        const float px = qi.x - qj.x, py = qi.y - qj.y, pz = qi.z - qj.z;
+        sx += c * px; sy += c * py; sz += c * pz;
+        const float G = kG(dist, invd, invh, p.cubic);
+        const float cv = 0.5f * (vi.w + vj.w) / aj.x * (px * dx + py * dy + pz * dz) / (d2 + eps_h2) * G / (dist + kFltEps);
+        vx -= cv * dx; vy -= cv * dy; vz -= cv * dz;
+    }
+    const float vs = 10.0f * p.rho0 * p.visc / ai.x;
+    const float f1 = 1.0f + factor;
+    return make_float3(qi.x * f1 + p.dt * (sx + vs * vx), qi.y * f1 + p.dt * (sy + vs * vy), qi.z * f1 + p.dt * (sz + vs * vz));
+}
+
+// A x0 with factor 0; r = b - A x0; p = r (MPSSolver.cuh:24-28).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const Scene& sc = d.scenes[block_scene(d, BS)];
+    if (i >= sc.slot_begin + sc.n) return;
+    const float3 a = apply_A(d, p, i, d.cg_x, 0.0f);
+    const float4 b = d.cg_b[i];
+    const float4 r = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
+    d.cg_r[i] = r;
+    d.cg_p[i] = r;
+}
+
+// A p, dots r.r and p.Ap in FP64, convergence decision and step length (MPSSolver.cuh:33-49).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long long cond, int use_cond) {
+    __shared__ double sh[32];
+    const int s = block_scene(d, BS);
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    double rr = 0.0, pap = 0.0;
+    if (i < sc.slot_begin + sc.n) {
+        const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor);
+        d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
+        const float4 r = d.cg_r[i];
+        const float4 q = d.cg_p[i];
+        rr = double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+        pap = double(q.x) * a.x + double(q.y) * a.y + double(q.z) * a.z;
+    }
+    const double b0 = block_sum<BS>(rr, sh);
+    const double b1 = block_sum<BS>(pap, sh);
+    if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = b0; d.partial[2 * blockIdx.x + 1] = b1; }
+    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
+    const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
+    const double tpap = scene_partial_sum<BS>(d, sc, 1, sh);
+    if (threadIdx.x == 0) {
+        SceneSolve& S = d.solve[s];
+        const int l = S.iter;
+        const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
+        const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
+        S.err = trr;
+        S.rr = trr;
+        if (stop) {
+            S.active = 0;
+            S.do_update = 0;
+        } else {
+            S.do_update = 1;
+            S.cg_alpha = trr / tpap;
+            S.iter = l + 1;
+            if (l + 1 > cap) S.active = 0;
+        }
+        finish_scene_decision(d, p, cond, use_cond);
+    }
+}
+
+// x += alpha p; r -= alpha Ap; beta = (r.r)_new / (r.r)_old (MPSSolver.cuh:49-60).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p) {
+    __shared__ double sh[32];
+    const int s = block_scene(d, BS);
+    if (!d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    double rr = 0.0;
+    if (i < sc.slot_begin + sc.n) {
+        const float a = float(d.solve[s].cg_alpha);
+        float4 x = d.cg_x[i];
+        float4 r = d.cg_r[i];
+        const float4 q = d.cg_p[i];
+        const float4 ap = d.cg_ap[i];
+        x.x += a * q.x; x.y += a * q.y; x.z += a * q.z;
+        r.x -= a * ap.x; r.y -= a * ap.y; r.z -= a * ap.z;
+        d.cg_x[i] = x;
+        d.cg_r[i] = r;
+        rr = double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+    }
+    const double b0 = block_sum<BS>(rr, sh);
+    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = b0;
+    if (!last_block_of_scene<BS>(d, s, sc)) return;
+    const double t = scene_partial_sum<BS>(d, sc, 0, sh);
+    if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
+}
+
+// p = r + beta p (MPSCGKernel.cuh:196-207).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_dir(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+    if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int s = block_scene(d, BS);
+    if (!d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    if (i >= sc.slot_begin + sc.n) return;
+    const float b = float(d.solve[s].cg_beta);
+    const float4 r = d.cg_r[i];
+    float4 q = d.cg_p[i];
+    q.x = r.x + b * q.x; q.y = r.y + b * q.y; q.z = r.z + b * q.z;
+    d.cg_p[i] = q;
+}
+
+// v = x (copy predictVel back, MPSSPHNonPressureUtil.cu:177-180).
+__global__ void k_cg_finish(Dev d, Params p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    const Scene& sc = d.scenes[d.chunk_scene[i / kChunk]];
+    if (i >= sc.slot_begin + sc.n) return;
+    const float4 x = d.cg_x[i];
+    float4 v = d.vel[i];
+    v.x = x.x; v.y = x.y; v.z = x.z;
+    d.vel[i] = v;
+}
+
+// ------------------------------------------------------------------ advection
+__device__ __forceinline__ float collide(float pos, float lo, float hi, float v) {
+    if (pos < lo && v < 0.0f) return fabsf(v) < 1.0e-4f ? 0.0f : -v * 0.4f;
+    if (pos > hi && v > 0.0f) return fabsf(v) < 1.0e-4f ? 0.0f : -v * 0.4f;
+    return v;
+}
+
+__global__ void k_advect(Dev d, Params p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    const Scene& sc = d.scenes[d.chunk_scene[i / kChunk]];
+    if (i >= sc.slot_begin + sc.n) return;
+    float4 x = d.pos[i];
+    float4 v = d.vel[i];
+    v.x = collide(x.x + v.x * p.dt, sc.bminx, sc.bmaxx, v.x);
+    v.y = collide(x.y + v.y * p.dt, sc.bminy, sc.bmaxy, v.y);
+    v.z = collide(x.z + v.z * p.dt, sc.bminz, sc.bmaxz, v.z);
+    x.x += p.dt * v.x; x.y += p.dt * v.y; x.z += p.dt * v.z;
+    d.pos[i] = x;
+    d.vel[i] = v;
+}
+
+// Loads a state given in particle-ID order (pos4.w = particle radius) into the slot layout.
+__global__ void k_load_state(Dev d, Params p, const float4* __restrict__ pos4, const float4* __restrict__ vel4, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int lo = 0, hi = p.nscenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.scenes[mid].coff <= k) lo = mid; else hi = mid - 1;
+    }
+    const Scene& sc = d.scenes[lo];
+    const int slot = sc.slot_begin + (k - sc.coff);
+    float4 x = pos4[k];
+    x.w *= kHRatio;
+    d.pos[slot] = x;
+    d.vel[slot] = vel4[k];
+    d.ids[slot] = unsigned(k);
+}
+
+// Stores the state in particle-ID order (pos4.w = particle radius).
+__global__ void k_store_state(Dev d, Params p, float4* __restrict__ pos4, float4* __restrict__ vel4) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    const Scene& sc = d.scenes[d.chunk_scene[i / kChunk]];
+    if (i >= sc.slot_begin + sc.n) return;
+    const unsigned id = d.ids[i];
+    float4 x = d.pos[i];
+    x.w *= (1.0f / kHRatio);
+    if (pos4) pos4[id] = x;
+    if (vel4) vel4[id] = d.vel[i];
+}
+
+int nblocks_for(int n, int bs) { return (n + bs - 1) / bs; }
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+#define MPSG_BS_SWITCH(bs, KERNEL, ...)                                                      \
+    do {                                                                                     \
+        if ((bs) == 128) KERNEL<128><<<p.slots / 128, 128, 0, s>>>(__VA_ARGS__);             \
+        else if ((bs) == 64) KERNEL<64><<<p.slots / 64, 64, 0, s>>>(__VA_ARGS__);            \
+        else KERNEL<256><<<p.slots / 256, 256, 0, s>>>(__VA_ARGS__);                         \
+    } while (0)
+
+void launch_keys(const Dev& d, const Params& p, cudaStream_t s) {
+    k_keys<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
+}
+void launch_reorder(const Dev& d, const Params& p, int n_real, cudaStream_t s) {
+    if (n_real > 0) k_reorder<<<nblocks_for(n_real, 256), 256, 0, s>>>(d, p, n_real);
+}
+void launch_build_nbrs(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_build_nbrs, d, p);
+}
+void launch_bvolume(const Dev& d, const Params& p, int nb, int accumulate, cudaStream_t s) {
+    if (nb > 0) k_bvolume<<<nblocks_for(nb, 256), 256, 0, s>>>(d, p, nb, accumulate);
+}
+void launch_density_alpha(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_density_alpha, d, p);
+}
+void launch_solver_init(const Dev& d, const Params& p, cudaStream_t s) {
+    k_solver_init<<<1, 256, 0, s>>>(d, p);
+}
+void launch_set_cond(const Dev& d, unsigned long long cond, cudaStream_t s) {
+    k_set_cond<<<1, 1, 0, s>>>(d, cond);
+}
+void launch_pressure_A(const Dev& d, const Params& p, int mode, int bs, unsigned long long cond, int use_cond,
+                       cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_pressure_A, d, p, mode, cond, use_cond);
+}
+void launch_pressure_B(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                       cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_pressure_B, d, p, 0, cond, use_cond, limit);
+}
+void launch_pressure_B_profile(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_pressure_B, d, p, 1, 0ull, 0, 0);
+}
+void launch_solver_finish(const Dev& d, const Params& p, int which, cudaStream_t s) {
+    k_solver_finish<<<1, 256, 0, s>>>(d, p, which);
+}
+void launch_st_factor(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_st_factor, d, p);
+}
+void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_b, d, p);
+}
+void launch_cg_ax0(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_ax0, d, p);
+}
+void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
+}
+void launch_cg_update(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_update, d, p);
+}
+void launch_cg_dir(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                   cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_dir, d, p, cond, use_cond, limit);
+}
+void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s) {
+    k_cg_finish<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
+}
+void launch_load_state(const Dev& d, const Params& p, const float4* pos4, const float4* vel4, int n, cudaStream_t s) {
+    if (n > 0) k_load_state<<<nblocks_for(n, 256), 256, 0, s>>>(d, p, pos4, vel4, n);
+}
+void launch_store_state(const Dev& d, const Params& p, float4* pos4, float4* vel4, cudaStream_t s) {
+    k_store_state<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p, pos4, vel4);
+}
+void launch_advect(const Dev& d, const Params& p, cudaStream_t s) {
+    k_advect<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
+}
+
+}  // namespace mpsg

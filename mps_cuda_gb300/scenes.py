@@ -1,0 +1,220 @@
+"""Scene and configuration table.
+
+Scenes are built with the library's deterministic generators (mps_gen_block / mps_gen_box_walls /
+mps_gen_sphere) so that every implementation (this package, the FP64 oracle, the reference's own
+CUDA step) gets bit-identical inputs.
+
+- ``reference_surface_tension``: the reference's active scene, mps::System::SurfaceTensionTestScene
+  (src/MPS_System/MPSSystem.cpp:552-651) with the constants of System::Initalize (:26-72); its
+  mesh-sampled cube boundary (cube.obj, not shipped with the reference) is replaced by the box walls
+  sampled at the reference's boundary spacing 2 * (0.25 * 0.4) (MPSParticleSamplingUtil.cuh:31).
+- ``dam_break_32k`` / ``dam_break_1m``: the plain FP32 dam breaks (32^3 fluid in a unit box; 100^3
+  fluid in a 3 x 1.5 x 2 tank, y up, open top, ~210k wall particles).
+- ``colliding_4m``: two 2M-particle blocks at +-1 m/s around a sampled sphere in a 4 x 2 x 2 tank.
+- ``batched_256``: 256 independent dam breaks, fluid counts log-uniform in [2k, 64k].
+- ``adjoint_16k``: 32 x 32 x 16 block in a unit box, 30 fixed solver iterations.
+
+Material of the physical configs: rest density 1000, particle volume V = spacing^3 (so the rest
+lattice sums to about rho0), mass = rho0 V, viscosity 0.01, surface tension 0.05, XSPH 0.1 (the
+reference default), cubic spline kernel, tolerances 0.1 % density and 0.1 % divergence.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+FACE_NX, FACE_PX, FACE_NY, FACE_PY, FACE_NZ, FACE_PZ = (1 << k for k in range(6))
+
+
+@dataclass
+class Scene:
+    name: str
+    pos4: np.ndarray            # (N, 4) float32: x, y, z, particle radius
+    vel4: np.ndarray            # (N, 4) float32: vx, vy, vz, mass
+    bpos4: np.ndarray           # (B, 4) float32: x, y, z, particle radius
+    material: dict
+    physics: dict
+    config: dict = field(default_factory=dict)
+    steps: int = 1
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos4.shape[0])
+
+    @property
+    def nb(self) -> int:
+        return int(self.bpos4.shape[0])
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def gen_block(dims, origin, spacing, radius, mass, jitter, seed):
+    lib = L.load()
+    nx, ny, nz = (int(d) for d in dims)
+    n = nx * ny * nz
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    o = (C.c_double * 3)(*origin)
+    L.check(lib.mps_gen_block(nx, ny, nz, o, spacing, radius, mass, jitter, seed, _ptr(pos), _ptr(vel)))
+    return pos, vel
+
+
+def gen_walls(lo, hi, spacing, radius, open_mask=0):
+    lib = L.load()
+    clo, chi = (C.c_double * 3)(*lo), (C.c_double * 3)(*hi)
+    n = lib.mps_gen_box_walls(clo, chi, spacing, radius, open_mask, None)
+    if n < 0:
+        raise ValueError("bad wall arguments")
+    out = np.zeros((n, 4), np.float32)
+    lib.mps_gen_box_walls(clo, chi, spacing, radius, open_mask, _ptr(out))
+    return out
+
+
+def gen_sphere(center, R, spacing, radius):
+    lib = L.load()
+    c = (C.c_double * 3)(*center)
+    n = lib.mps_gen_sphere(c, R, spacing, radius, None)
+    out = np.zeros((n, 4), np.float32)
+    lib.mps_gen_sphere(c, R, spacing, radius, _ptr(out))
+    return out
+
+
+def physical_material(spacing: float, rho0: float = 1000.0, visc: float = 0.01, sigma: float = 0.05,
+                      xsph: float = 0.1, radius: float | None = None) -> dict:
+    V = spacing ** 3
+    r = radius if radius is not None else spacing / 2
+    return dict(radius=4 * r, mass=rho0 * V, density=rho0, volume=V, viscosity=visc, xsph=xsph, surface_tension=sigma)
+
+
+def reference_material(h: float, density: float = 1.0) -> dict:
+    """SPHMaterial() + SetRadius(h) (MPSSPHMaterial.cpp:4-19)."""
+    V = h * h * h / 48.0 * 3.141592
+    return dict(radius=h, mass=density * V, density=density, volume=V, viscosity=0.025, xsph=0.1,
+                surface_tension=100.0)
+
+
+PHYS_CONFIG = dict(kernel=L.KERNEL_CUBIC_SPLINE, df_tol=1.0e-3, cd_tol=1.0e-3, df_min_iter=1, cd_min_iter=2,
+                   max_iter=100)
+
+
+def dam_break(dims, spacing, radius, jitter, lo, hi, open_mask=0, seed=0, dt=1.0e-3, name="dam_break",
+              steps=1, origin=None, wall_spacing=None, material=None, config=None) -> Scene:
+    mat = material or physical_material(spacing, radius=radius)
+    org = origin if origin is not None else lo
+    pos, vel = gen_block(dims, org, spacing, radius, mat["mass"], jitter, seed)
+    walls = gen_walls(lo, hi, wall_spacing or spacing, radius, open_mask)
+    phys = dict(dt=dt, gravity=(0.0, -9.81, 0.0), min=tuple(lo), max=tuple(hi))
+    cfg = dict(PHYS_CONFIG)
+    cfg.update(config or {})
+    return Scene(name, pos, vel, walls, mat, phys, cfg, steps, dict(dims=tuple(dims), spacing=spacing, seed=seed))
+
+
+def dam_break_32k(seed: int = 0) -> Scene:
+    return dam_break((32, 32, 32), 0.02, 0.01, 0.002, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), seed=seed, dt=1.0e-3,
+                     name="dam_break_32k", steps=1000)
+
+
+def dam_break_1m(seed: int = 0) -> Scene:
+    return dam_break((100, 100, 100), 0.01, 0.005, 0.001, (0.0, 0.0, 0.0), (3.0, 1.5, 2.0), open_mask=FACE_PY,
+                     seed=seed, dt=5.0e-4, name="dam_break_1m", steps=2000)
+
+
+def dam_break_small(n: int = 10, seed: int = 0, box: float = 0.5, kernel=L.KERNEL_CUBIC_SPLINE) -> Scene:
+    """Small dam break with the dam_break_32k constants (for tests)."""
+    return dam_break((n, n, n), 0.02, 0.01, 0.002, (0.0, 0.0, 0.0), (box, box, box), seed=seed, dt=1.0e-3,
+                     name=f"dam_break_{n}", config=dict(kernel=kernel))
+
+
+def colliding_4m(seed: int = 0, scale: float = 1.0) -> Scene:
+    """Two blocks (128 x 125 x 125 each at full scale) at +-1 m/s around a sampled sphere."""
+    sp, r = 0.01, 0.005
+    mat = physical_material(sp, radius=r)
+    d = (max(2, round(128 * scale)), max(2, round(125 * scale)), max(2, round(125 * scale)))
+    ext = [sp * (k + 1) for k in d]
+    lo, hi = (0.0, 0.0, 0.0), (4.0, 2.0, 2.0)
+    yz0 = (1.0 - ext[1] / 2, 1.0 - ext[2] / 2)
+    pa, va = gen_block(d, (2.0 - 0.25 - ext[0], yz0[0], yz0[1]), sp, r, mat["mass"], 0.001, seed)
+    pb, vb = gen_block(d, (2.0 + 0.25 - sp, yz0[0], yz0[1]), sp, r, mat["mass"], 0.001, seed + 1)
+    va[:, 0] = 1.0
+    vb[:, 0] = -1.0
+    walls = gen_walls(lo, hi, sp, r)
+    sph = gen_sphere((2.0, 1.0, 1.0), 0.2, sp, r)
+    phys = dict(dt=5.0e-4, gravity=(0.0, -9.81, 0.0), min=lo, max=hi)
+    return Scene("colliding_4m", np.concatenate([pa, pb]), np.concatenate([va, vb]), np.concatenate([walls, sph]),
+                 mat, phys, dict(PHYS_CONFIG), 500, dict(dims=d, seed=seed))
+
+
+def batched_scenes(nscenes: int = 256, seed: int = 0, nmin: int = 2000, nmax: int = 64000) -> list[Scene]:
+    """Independent dam breaks: N log-uniform in [nmin, nmax], aspect U[0.5, 2], box 1.5-3x the block."""
+    rng = np.random.default_rng(seed)
+    out = []
+    sp, r = 0.02, 0.01
+    for s in range(nscenes):
+        n = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        b, c = rng.uniform(0.5, 2.0, size=2)
+        nx = max(2, round((n / (b * c)) ** (1.0 / 3.0)))
+        dims = (nx, max(2, round(nx * b)), max(2, round(nx * c)))
+        ext = [sp * (k + 1) for k in dims]
+        f = rng.uniform(1.5, 3.0, size=3)
+        hi = tuple(float(ext[a] * f[a]) for a in range(3))
+        out.append(dam_break(dims, sp, r, 0.002, (0.0, 0.0, 0.0), hi, seed=seed * 1000003 + s, dt=1.0e-3,
+                             name=f"batched_{s}"))
+    return out
+
+
+def adjoint_16k(seed: int = 0) -> Scene:
+    sc = dam_break((32, 32, 16), 0.02, 0.01, 0.002, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), seed=seed, dt=1.0e-3,
+                   name="adjoint_16k", steps=200, config=dict(fixed_iters=30))
+    rng = np.random.default_rng(seed + 17)
+    sc.vel4[:, :3] = rng.normal(0.0, 0.1, size=(sc.n, 3)).astype(np.float32)
+    return sc
+
+
+def reference_surface_tension(size: int = 5) -> Scene:
+    """mps::System::SurfaceTensionTestScene (MPSSystem.cpp:552-651) with Initalize's constants."""
+    radius = 0.1
+    f32 = lambda v: float(np.float32(v))  # the reference writes 0.9f and 0.001f literals
+    gap = radius * f32(0.9)
+    offset = f32(0.001)
+    stride = gap + gap + offset
+    l = stride * (size - 1) + gap + gap
+    start = -l
+    lo = (start - l * 0.025 + gap - 3.5, start + gap - 3.5, start + gap - 3.5)
+    hi = (l * 0.025 + (size - 1) * stride + gap + 3.5, start + (size - 1) * stride + gap + 3.5,
+          start + (size - 1) * stride + gap + 3.5)
+    mat = reference_material(4 * radius)
+    pos = []
+    for z in range(size):
+        for y in range(size):
+            for x in range(size):
+                pos.append((start - l * 0.025 + x * stride + gap, start + y * stride + gap, start + z * stride + gap))
+                pos.append((l * 0.025 + x * stride + gap, start + y * stride + gap, start + z * stride + gap))
+    pos = np.array(pos, np.float64)
+    n = pos.shape[0]
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = pos
+    pos4[:, 3] = radius
+    vel4 = np.zeros((n, 4), np.float32)
+    vel4[:, 3] = mat["mass"]
+    walls = gen_walls(lo, hi, 2 * (0.25 * mat["radius"]), 0.25 * mat["radius"])
+    phys = dict(dt=0.005, gravity=(0.0, -9.8, 0.0), min=lo, max=hi)
+    cfg = dict(kernel=L.KERNEL_POLY6_SPIKY)
+    return Scene("reference_surface_tension", pos4, vel4, walls, mat, phys, cfg, 1,
+                 dict(pos_f64=pos, hash_cell=4 * radius, hash_size=(64, 64, 64)))
+
+
+CONFIGS = {
+    "dam_break_32k": dam_break_32k,
+    "dam_break_1m": dam_break_1m,
+    "colliding_4m": colliding_4m,
+    "adjoint_16k": adjoint_16k,
+    "reference_surface_tension": reference_surface_tension,
+}

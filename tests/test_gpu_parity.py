@@ -1,0 +1,256 @@
+"""Parity of the CUDA step (through the C ABI) against the FP64 oracle.
+
+Tolerances (FP32 bulk vs FP64 oracle, same inputs):
+  - integer work (cell keys, sort permutation, cell ranges, FP32 neighbour counts): bit-exact
+    against the oracle's restatement of the same FP32 scheme; neighbour counts against the
+    reference's FP64 test differ only for pairs within 1e-6 h of the support radius.
+  - densities, alphas, pressure factors, velocities after a phase, from an identical state:
+    max|a - b| / max|b| <= 1e-5 (the north-star bound "1e-5 relative of an FP64 oracle").
+Solver phases are compared in fixed-iteration mode (same number of Jacobi / CG iterations on
+both sides) and, in adaptive mode, by iteration counts within one iteration.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def make(mps, orc, scene, **cfg):
+    from mps_cuda_gb300 import Simulation
+    sim = Simulation.from_scene(scene, **cfg)
+    o = orc.from_scene(scene, config=cfg)
+    return sim, o
+
+
+def advance_to_density(sim, o, mps):
+    sim.phase(mps.PHASE_SORT)
+    sim.phase(mps.PHASE_NEIGHBORS)
+    sim.phase(mps.PHASE_BVOLUME)
+    sim.phase(mps.PHASE_DENSITY_ALPHA)
+    for ph in (0, 1, 2, 3, 4, 5):  # zsort(no-op), neighbours, volume, density, alpha, gravity
+        o.phase(ph)
+
+
+@pytest.fixture(params=["cubic", "poly6"])
+def small(request, mps):
+    from mps_cuda_gb300 import scenes
+    k = mps.KERNEL_CUBIC_SPLINE if request.param == "cubic" else mps.KERNEL_POLY6_SPIKY
+    return scenes.dam_break_small(10, seed=5, kernel=k)
+
+
+def test_sort_keys_and_ranges_bit_exact(mps, orc):
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(12, seed=2)
+    sim = Simulation.from_scene(sc)
+    sim.phase(mps.PHASE_SORT)
+    g = sim.grid()
+    grid = orc.grid(g["origin"], g["cell"], g["dims"])
+    q4 = sc.pos4.copy()
+    q4[:, 3] *= 4
+    keys = orc.new_keys(q4, grid)
+    sk, order = orc.new_stable_sort(keys, np.arange(sc.n, dtype=np.uint32))
+    gpu_keys = sim.get_field("cell_key", order="slot")
+    gpu_ids = sim.get_field("ids", order="slot")
+    assert np.array_equal(gpu_keys, sk)
+    assert np.array_equal(gpu_ids, order)
+    # positions were moved with their particles
+    assert np.array_equal(sim.get_field("pos", order="id")[:, :3], sc.pos4[:, :3])
+
+
+def test_neighbour_counts_bit_exact(mps, orc, small):
+    sc = small
+    from mps_cuda_gb300 import Simulation
+    sim = Simulation.from_scene(sc)
+    sim.phase(mps.PHASE_SORT)
+    sim.phase(mps.PHASE_NEIGHBORS)
+    g = sim.grid()
+    grid = orc.grid(g["origin"], g["cell"], g["dims"])
+    q4 = sc.pos4.copy(); q4[:, 3] *= 4
+    b4 = sc.bpos4.copy(); b4[:, 3] *= 4
+    kq_s, order = orc.new_stable_sort(orc.new_keys(q4, grid), np.arange(sc.n, dtype=np.uint32))
+    kb_s, border = orc.new_stable_sort(orc.new_keys(b4, grid), np.arange(sc.nb, dtype=np.uint32))
+    cf = orc.new_nbr_counts(q4[order], q4[order], kq_s, grid, True)
+    cb = orc.new_nbr_counts(q4[order], b4[border], kb_s, grid, False)
+    c = sim.get_field("nbr_count", order="slot")
+    assert np.array_equal(c & 0xFFFF, cf)
+    assert np.array_equal(c >> 16, cb)
+    st = sim.stats()
+    assert st["fluid_pairs"] == int(cf.sum()) and st["boundary_pairs"] == int(cb.sum())
+    # against the reference's FP64 criterion
+    o = orc.from_scene(sc)
+    o.phase(orc.NEIGHBORS)
+    ref = np.diff(o.get("nei_ff_idx"))
+    gpu = sim.get_field("nbr_count", order="id") & 0xFFFF
+    assert (gpu != ref).sum() <= max(1, sc.n // 10000)
+
+
+def test_boundary_volume(mps, orc, small):
+    sim, o = make(mps, orc, small)
+    o.phase(orc.NEIGHBORS)
+    o.phase(orc.BVOLUME)
+    assert rel_err(sim.get_field("bvol", order="id"), o.get("bvol")) < REL
+
+
+def test_density_alpha_gravity(mps, orc, small):
+    sim, o = make(mps, orc, small)
+    advance_to_density(sim, o, mps)
+    assert rel_err(sim.get_field("density"), o.get("density")) < REL
+    assert rel_err(sim.get_field("alpha"), o.get("alpha")) < REL
+    assert np.abs(sim.get_field("color") - o.get("color")).max() < 1e-5
+    assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL
+
+
+@pytest.mark.parametrize("fixed", [0, 4])
+def test_pressure_and_nonpressure_solves(mps, orc, small, fixed):
+    sim, o = make(mps, orc, small, fixed_iters=fixed)
+    advance_to_density(sim, o, mps)
+    # from an identical state: the oracle's velocities go into the GPU before each solve
+    for gph, oph, name in ((mps.PHASE_DF, orc.DF, "df_iters"), (mps.PHASE_VISCST, orc.VISCST, "cg_iters"),
+                           (mps.PHASE_CD, orc.CD, "cd_iters")):
+        v = sim.get_field("vel")
+        v[:, :3] = o.get("vel")
+        sim.put_field("vel", v)
+        sim.phase(gph)
+        o.phase(oph)
+        gi, oi = sim.stats()[name], o.stats()[name]
+        if fixed:
+            assert gi == oi == fixed + 1, (name, gi, oi)
+        else:
+            assert abs(gi - oi) <= 1, (name, gi, oi)
+        if gi == oi:
+            assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL, name
+    if fixed:
+        assert rel_err(sim.get_field("pressure"), o.get("pressure")) < 1e-4
+
+
+def test_advect(mps, orc, small):
+    sim, o = make(mps, orc, small, fixed_iters=3)
+    advance_to_density(sim, o, mps)
+    for gph, oph in ((mps.PHASE_DF, orc.DF), (mps.PHASE_VISCST, orc.VISCST), (mps.PHASE_CD, orc.CD)):
+        sim.phase(gph)
+        o.phase(oph)
+    v = sim.get_field("vel")
+    v[:, :3] = o.get("vel")
+    sim.put_field("vel", v)
+    sim.phase(mps.PHASE_ADVECT)
+    o.phase(orc.ADVECT)
+    assert rel_err(sim.get_field("pos")[:, :3], o.get("pos")) < 1e-6
+    assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL
+
+
+def test_graph_step_equals_eager_phases(mps):
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(10, seed=9)
+    a = Simulation.from_scene(sc, use_graph=1)
+    b = Simulation.from_scene(sc, use_graph=0)
+    a.step(3)
+    b.step(3)
+    pa, va = a.get_fluid()
+    pb, vb = b.get_fluid()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    assert a.stats() ["cd_iters"] == b.stats()["cd_iters"]
+
+
+def test_deterministic(mps):
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(10, seed=4)
+    outs = []
+    for _ in range(2):
+        s = Simulation.from_scene(sc)
+        s.step(4)
+        outs.append(s.get_fluid())
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_full_step_vs_oracle_fixed_iterations(mps, orc, small):
+    sim, o = make(mps, orc, small, fixed_iters=5)
+    sim.step(1)
+    o.step(1)
+    p, v = sim.get_fluid()
+    assert rel_err(p[:, :3], o.get("pos")) < 1e-6
+    assert rel_err(v[:, :3], o.get("vel")) < 1e-4
+    assert rel_err(sim.get_field("density"), o.get("density")) < REL
+
+
+def test_reference_scene_step(mps, orc):
+    """The reference's own scene (poly6/spiky, reference material, shipped tolerances)."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.reference_surface_tension()
+    sim = Simulation.from_scene(sc)
+    o = orc.from_scene(sc)
+    for f in range(3):
+        sim.step(1)
+        o.step(1)
+        st, ost = sim.stats(), o.stats()
+        assert abs(st["df_iters"] - ost["df_iters"]) <= 1
+        assert abs(st["cd_iters"] - ost["cd_iters"]) <= 2
+    p, v = sim.get_fluid()
+    assert rel_err(p[:, :3], o.get("pos")) < 1e-4
+
+
+def test_batched_equals_single(mps):
+    from mps_cuda_gb300 import BatchedSimulation, Simulation, scenes
+    scs = scenes.batched_scenes(4, seed=3, nmin=500, nmax=3000)
+    b = BatchedSimulation(scs)
+    b.step(2)
+    pb, vb = b.get_fluid()
+    its = b.scene_iters()
+    off = 0
+    for k, sc in enumerate(scs):
+        s = Simulation.from_scene(sc)
+        s.step(2)
+        p, v = s.get_fluid()
+        assert np.array_equal(p, pb[off:off + sc.n]) and np.array_equal(v, vb[off:off + sc.n]), k
+        st = s.stats()
+        assert (st["df_iters"], st["cg_iters"], st["cd_iters"]) == tuple(its[k])
+        off += sc.n
+
+
+def test_step_host_matches_device_step(mps):
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(8, seed=6)
+    a = Simulation.from_scene(sc)
+    b = Simulation.from_scene(sc)
+    a.step(2)
+    p = sc.pos4.copy()
+    v = sc.vel4.copy()
+    b.step_host(p, v, 1)
+    b.step_host(p, v, 1)
+    pa, va = a.get_fluid()
+    assert np.allclose(p, pa, atol=0, rtol=0) or rel_err(p[:, :3], pa[:, :3]) < 1e-6
+
+
+def test_overflow_and_nonfinite_are_reported(mps):
+    from mps_cuda_gb300 import MpsError, Simulation, scenes
+    sc = scenes.dam_break_small(6, seed=1)
+    s = Simulation.from_scene(sc, max_fluid_neighbors=4)
+    s.step(1)
+    with pytest.raises(MpsError, match="OVERFLOW"):
+        s.stats()
+    sc2 = scenes.dam_break_small(6, seed=1)
+    sc2.pos4[5, 0] = np.nan
+    s2 = Simulation.from_scene(sc2)
+    s2.step(1)
+    with pytest.raises(MpsError, match="NONFINITE"):
+        s2.stats()
+
+
+def test_empty_boundary_and_out_of_box_particles(mps, orc):
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(6, seed=8)
+    sc.bpos4 = sc.bpos4[:0]
+    sc.pos4[0, :3] = (-0.3, 0.1, 0.1)   # outside the box: clamped into the border cells
+    sim = Simulation.from_scene(sc, fixed_iters=3)
+    o = orc.from_scene(sc, config=dict(fixed_iters=3))
+    sim.step(1)
+    o.step(1)
+    p, v = sim.get_fluid()
+    assert rel_err(p[:, :3], o.get("pos")) < 1e-6
