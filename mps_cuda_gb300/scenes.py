@@ -127,6 +127,12 @@ def dam_break_1m(seed: int = 0) -> Scene:
                      seed=seed, dt=5.0e-4, name="dam_break_1m", steps=2000)
 
 
+def dam_break_512k(seed: int = 0) -> Scene:
+    """80^3 fluid in the 1M dam break's tank (profiling size: working set just above L2)."""
+    return dam_break((80, 80, 80), 0.01, 0.005, 0.001, (0.0, 0.0, 0.0), (3.0, 1.5, 2.0), open_mask=FACE_PY,
+                     seed=seed, dt=5.0e-4, name="dam_break_512k", steps=2000)
+
+
 def dam_break_small(n: int = 10, seed: int = 0, box: float = 0.5, kernel=L.KERNEL_CUBIC_SPLINE) -> Scene:
     """Small dam break with the dam_break_32k constants (for tests)."""
     return dam_break((n, n, n), 0.02, 0.01, 0.002, (0.0, 0.0, 0.0), (box, box, box), seed=seed, dt=1.0e-3,
@@ -214,6 +220,7 @@ def reference_surface_tension(size: int = 5) -> Scene:
 CONFIGS = {
     "dam_break_32k": dam_break_32k,
     "dam_break_1m": dam_break_1m,
+    "dam_break_512k": dam_break_512k,
     "colliding_4m": colliding_4m,
     "adjoint_16k": adjoint_16k,
     "reference_surface_tension": reference_surface_tension,
