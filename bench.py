@@ -131,7 +131,7 @@ def run_ours(args, scene, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
-    sim = Simulation.from_scene(scene, device=local_rank)
+    sim = Simulation.from_scene(scene, device=local_rank, use_graph=0 if args.eager else 1)
 
     def barrier():
         if dist:
@@ -141,6 +141,7 @@ def run_ours(args, scene, rank, world, local_rank):
     sim.step(args.warmup, stream)
     torch.cuda.synchronize(dev)
     st0 = sim.stats()
+    snap_p, snap_v = sim.get_fluid(stream)  # e2e replays the same steps from this state
     barrier()
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -164,14 +165,13 @@ def run_ours(args, scene, rank, world, local_rank):
     P = radix_passes(sim)
     launches = sum(sim.launches_per_step((0, 0, 0), P) for _ in range(args.steps)) + 2 * runs[0] + 3 * runs[1] + 2 * runs[2]
 
-    # ---- e2e through the host-buffer C-ABI call (pinned H2D + step + D2H every step)
+    # ---- e2e through the host-buffer C-ABI call (pinned H2D + step + D2H every step), replaying
+    # the timed steps from the same starting state
     pin_p = torch.empty((scene.n, 4), dtype=torch.float32, pin_memory=True)
     pin_v = torch.empty((scene.n, 4), dtype=torch.float32, pin_memory=True)
-    p0, v0 = sim.get_fluid(stream)
-    pin_p.numpy()[:] = p0
-    pin_v.numpy()[:] = v0
-    e2e_steps = max(1, min(args.steps, 10))
-    sim.step_host(pin_p.numpy(), pin_v.numpy(), 1, stream)  # warm
+    e2e_steps = args.steps
+    pin_p.numpy()[:] = snap_p
+    pin_v.numpy()[:] = snap_v
     torch.cuda.synchronize(dev)
     barrier()
     t0 = time.perf_counter()
@@ -179,6 +179,11 @@ def run_ours(args, scene, rank, world, local_rank):
         sim.step_host(pin_p.numpy(), pin_v.numpy(), 1, stream)
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
+    t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if dist:
+        import torch.distributed as td
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+    e2e_s = float(t.item())
     e2e = {"value": scene.n * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 32 * scene.n,
            "d2h_bytes_per_step": 32 * scene.n, "steps": e2e_steps}
 
@@ -224,6 +229,77 @@ def run_ours(args, scene, rank, world, local_rank):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene)
+    if dist:
+        import torch.distributed as td
+        td.destroy_process_group()
+    return line
+
+
+def run_batched(args, scenes_list, rank, world, local_rank):
+    """256 independent scenes: one set of launches per pass over all scenes (CUDA graph, device
+    loops that run until every scene has converged) vs. the same scenes stepped one by one."""
+    import torch
+    from mps_cuda_gb300 import BatchedSimulation, Simulation, build
+    from mps_cuda_gb300.sharding import partition_scenes
+    build.build()
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    mine = partition_scenes([s.n for s in scenes_list], world)[rank]
+    local = [scenes_list[i] for i in mine]
+    n_local = sum(s.n for s in local)
+    sim = BatchedSimulation(local, device=local_rank)
+    sim.step(args.warmup, stream)
+    torch.cuda.synchronize(dev)
+    if dist:
+        import torch.distributed as td
+        td.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        sim.step(args.steps, stream)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    tot = torch.tensor([n_local], dtype=torch.float64, device=dev)
+    if dist:
+        import torch.distributed as td
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        td.all_reduce(tot)
+    ms_max = float(t.item())
+    value = float(tot.item()) * args.steps / (ms_max / 1e3)
+    its = sim.scene_iters()
+    sim.close()
+    # the same scenes, one plain step each, launched one scene after the other
+    sims = [Simulation.from_scene(s, device=local_rank) for s in local]
+    for s in sims:
+        s.step(args.warmup, stream)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for s in sims:
+        s.step(1, stream)
+    e1.record(stream)
+    e1.synchronize()
+    per_ms = e0.elapsed_time(e1)
+    per_value = n_local / (per_ms / 1e3)
+    for s in sims:
+        s.close()
+    line = {
+        "metric": "particle-steps/s (DFSPH, 256 batched scenes)", "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched_256", "scenes": len(scenes_list), "fluid_particles": sum(s.n for s in scenes_list),
+                   "boundary_particles": sum(s.nb for s in scenes_list), "parallelism": "scenes split over ranks"},
+        "per_scene_launches": {"value": per_value, "unit": UNIT, "ms_for_all_scenes_one_step": per_ms},
+        "batched_over_per_scene": value / per_value,
+        "max_iterations": {"df": int(its[:, 0].max()), "cg": int(its[:, 1].max()), "cd": int(its[:, 2].max())},
+        "clocks": clk.summary(),
+    }
     if dist:
         import torch.distributed as td
         td.destroy_process_group()
@@ -276,10 +352,18 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="dam_break_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--eager", action="store_true",
+                    help="host-driven solver loops instead of the CUDA graph (same kernels; for ncu, which "
+                         "cannot profile kernels of graphs with conditional nodes)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local_rank = env_rank()
     from mps_cuda_gb300 import scenes
+    if args.config == "batched_256":
+        line = run_batched(args, scenes.batched_scenes(256, seed=0), rank, world, local_rank)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     scene = scenes.CONFIGS[args.config](seed=rank) if args.config != "reference_surface_tension" else \
         scenes.reference_surface_tension()
     if args.impl == "reference":

@@ -19,7 +19,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mps_c.h"
+#include "mps_c.h"
 #include "mps_internal.cuh"
 
 using namespace mpsg;
@@ -98,6 +98,7 @@ struct mps_handle {
     float2* aux = nullptr;
     float4* color = nullptr;
     float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr;
+    float2* cg_coef = nullptr;
     float4* bpos = nullptr;
     float* bvol = nullptr;
     double* partial = nullptr;
@@ -140,7 +141,8 @@ void mps_handle::release() {
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
                      (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&rho,
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
-                     (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&bpos, (void**)&bvol,
+                     (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_coef,
+                     (void**)&bpos, (void**)&bvol,
                      (void**)&partial, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
                      (void**)&keys, (void**)&keys_tmp, (void**)&vals, (void**)&vals_tmp, (void**)&sort_counts,
                      (void**)&stage_pos, (void**)&stage_vel};
@@ -228,6 +230,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.cg_p = h->cg_p;
     d.cg_ap = h->cg_ap;
     d.cg_b = h->cg_b;
+    d.cg_coef = h->cg_coef;
     d.bpos = h->bpos;
     d.bvol = h->bvol;
     d.partial = h->partial;
@@ -326,6 +329,7 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(cudaMemcpy(h->chunk_scene, chunk.data(), chunk.size() * sizeof(int), cudaMemcpyHostToDevice));
     MPS_CUDA_TRY(dalloc(&h->nbr_f, S * size_t(h->cfg.max_fluid_neighbors)));
     MPS_CUDA_TRY(dalloc(&h->nbr_b, S * size_t(h->cfg.max_boundary_neighbors)));
+    MPS_CUDA_TRY(dalloc(&h->cg_coef, S * size_t(h->cfg.max_fluid_neighbors)));
     MPS_CUDA_TRY(dalloc(&h->cnt, S));
     MPS_CUDA_TRY(cudaMemset(h->cnt, 0, S * sizeof(unsigned)));
     MPS_CUDA_TRY(dalloc(&h->rho, S));

@@ -92,6 +92,7 @@ struct Dev {
     float2* aux;                  // (rho, st factor) packed for the CG gathers
     float4* color;
     float4 *cg_x, *cg_r, *cg_p, *cg_ap, *cg_b;
+    float2* cg_coef;              // per fluid pair, interleaved like nbr_f: (c_ij, cv_ij) of the CG operator
     const float4* bpos;           // boundary (x, y, z, h)
     float* bvol;
     double* partial;              // per-block FP64 partial sums (2 per block)

@@ -9,7 +9,7 @@
 #include <cstdint>
 #include <cstring>
 
-#include "../../include/mps_c.h"
+#include "mps_c.h"
 
 namespace {
 

@@ -499,12 +499,12 @@ __global__ void __launch_bounds__(BS) k_st_factor(Dev d, Params p) {
     d.aux[i] = make_float2(d.rho[i], acc);
 }
 
-// g_ij of the surface-tension operator (MPSSPHNonPressureUtil.cuh:510-515).
-struct StPair {
-    float gij, w, G, dist;
-};
-
 // b_i = v_i + dt sigma / m_i sum_j -mbar_ij g_ij x_ij; x0 = v (MPSSPHNonPressureUtil.cuh:467-521).
+// The operator's per-pair coefficients depend only on positions, the pre-solve velocities, rho
+// and the ST factor, all fixed during the CG solve, so they are computed here once per solve:
+//   c_ij  = dt sigma / m_i * mbar_ij g_ij + XSPH / dt * m_j / rho_j W_ij     (ST + XSPH, :577-582)
+//   cv_ij = 10 rho0 mu / rho_i * (m_i + m_j) / 2 / rho_j / (d^2 + 0.01 h_i^2) * G_ij / (d + eps)
+//                                                                           (viscosity, :628-633)
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
@@ -515,6 +515,10 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     const float4 vi = d.vel[i];
     const float2 ai = d.aux[i];
     const float invh = 1.0f / xi.w;
+    const float eps_h2 = 0.01f * xi.w * xi.w;
+    const float st_scale = p.dt * p.sigma / vi.w;
+    const float xs_scale = p.xsph * p.inv_dt;
+    const float vs = 10.0f * p.rho0 * p.visc / ai.x;
     const int nf = int(d.cnt[i] & 0xffffu);
     float bx = 0.0f, by = 0.0f, bz = 0.0f;
     for (int k = 0; k < nf; ++k) {
@@ -531,55 +535,44 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
         const float stg = kSTG(dist, invd, invh);
         const float vdot = stg * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
         const float gij = (stw + p.dt * (vdot - (ai.y + aj.y) * invD * 0.5f * stw)) * invD;
-        const float c = 0.5f * (vi.w + vj.w) * gij;
+        const float mbar = 0.5f * (vi.w + vj.w);
+        const float c = mbar * gij;
         bx -= c * dx; by -= c * dy; bz -= c * dz;
+        const float w = kW(dist, invh, p.cubic);
+        const float G = kG(dist, invd, invh, p.cubic);
+        const float inv_rj = 1.0f / aj.x;
+        float2 cf;
+        cf.x = st_scale * c + xs_scale * (vj.w * inv_rj) * w;
+        cf.y = vs * mbar * inv_rj / (d2 + eps_h2) * G / (dist + kFltEps);
+        d.cg_coef[size_t(k) * stride + size_t(i)] = cf;
     }
-    const float sc_ = p.dt * p.sigma / vi.w;
-    d.cg_b[i] = make_float4(vi.x + sc_ * bx, vi.y + sc_ * by, vi.z + sc_ * bz, 0.0f);
+    d.cg_b[i] = make_float4(vi.x + st_scale * bx, vi.y + st_scale * by, vi.z + st_scale * bz, 0.0f);
     d.cg_x[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
 }
 
-// (A q)_i = q_i (1 + f) + dt (ST + XSPH + viscosity) (MPSSPHNonPressureUtil.cuh:523-648).
+// (A q)_i = q_i (1 + f) + dt [sum_j c_ij (q_i - q_j) - sum_j cv_ij ((q_i - q_j).x_ij) x_ij]
+// with the coefficients of k_cg_b (MPSSPHNonPressureUtil.cuh:523-648).
 __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, const float4* q, float factor) {
     const size_t stride = size_t(p.slots);
     const float4 xi = d.pos[i];
-    const float4 vi = d.vel[i];
-    const float2 ai = d.aux[i];
     const float4 qi = q[i];
-    const float hi = xi.w;
-    const float invh = 1.0f / hi;
-    const float eps_h2 = 0.01f * hi * hi;
     const int nf = int(d.cnt[i] & 0xffffu);
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;   // surface tension + XSPH, already scaled per pair
-    float vx = 0.0f, vy = 0.0f, vz = 0.0f;   // viscosity
-    const float st_scale = p.dt * p.sigma / vi.w;
-    const float xs_scale = p.xsph * p.inv_dt;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+        const size_t at = size_t(k) * stride + size_t(i);
+        const unsigned j = d.nbr_f[at];
+        const float2 cf = d.cg_coef[at];
         const float4 xj = d.pos[j];
-        const float4 vj = d.vel[j];
-        const float2 aj = d.aux[j];
         const float4 qj = q[j];
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const float invd = safe_rsqrt(d2);
-        const float dist = d2 * invd;
-        const float invD = 2.0f / (ai.x + aj.x);
-        const float stw = kSTW(dist, invh);
-        const float stg = kSTG(dist, invd, invh);
-        const float vdot = stg * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
-        const float gij = (stw + p.dt * (vdot - (ai.y + aj.y) * invD * 0.5f * stw)) * invD;
-        const float w = kW(dist, invh, p.cubic);
-        const float c = st_scale * 0.5f * (vi.w + vj.w) * gij + xs_scale * (vj.w / aj.x) * w;
         const float px = qi.x - qj.x, py = qi.y - qj.y, pz = qi.z - qj.z;
-        sx += c * px; sy += c * py; sz += c * pz;
-        const float G = kG(dist, invd, invh, p.cubic);
-        const float cv = 0.5f * (vi.w + vj.w) / aj.x * (px * dx + py * dy + pz * dz) / (d2 + eps_h2) * G / (dist + kFltEps);
-        vx -= cv * dx; vy -= cv * dy; vz -= cv * dz;
+        const float t = cf.y * (px * dx + py * dy + pz * dz);
+        sx += cf.x * px - t * dx;
+        sy += cf.x * py - t * dy;
+        sz += cf.x * pz - t * dz;
     }
-    const float vs = 10.0f * p.rho0 * p.visc / ai.x;
     const float f1 = 1.0f + factor;
-    return make_float3(qi.x * f1 + p.dt * (sx + vs * vx), qi.y * f1 + p.dt * (sy + vs * vy), qi.z * f1 + p.dt * (sz + vs * vz));
+    return make_float3(qi.x * f1 + p.dt * sx, qi.y * f1 + p.dt * sy, qi.z * f1 + p.dt * sz);
 }
 
 // A x0 with factor 0; r = b - A x0; p = r (MPSSolver.cuh:24-28).
