@@ -174,6 +174,20 @@ enum mps_kernel_id {
  * work being measured.  No counterpart in the reference (it has no device timers). */
 int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream, double* ms);
 
+/* Allocation-free cell sort (no counterpart in the reference).  For callers that cannot
+ * allocate device memory -- an application recording a stream capture, a plugin whose host owns
+ * the GPU allocator, a real-time loop that cannot afford an allocation's implicit device
+ * synchronisation.  Computes the step's 64-bit cell keys of n caller-owned particles (device
+ * float4 x,y,z,w; w unused) on the grid (origin, cell, dims) and stable-sorts them: keys_out[k]
+ * is the k-th smallest key, order_out[k] the index of that particle.  Scratch lives in one fixed
+ * device array inside the library (about 3.1 MB, held by every GPU that loads it until exit);
+ * n > MPS_NOALLOC_MAX_PARTICLES returns MPS_E_INVALID.  The first call on a device looks up that
+ * array with the device current: make it before any stream capture.  Calls that overlap on the
+ * GPU share the array and race; serialise them. */
+#define MPS_NOALLOC_MAX_PARTICLES 262144
+int mps_cell_sort_noalloc(const float* pos4, int64_t n, const float origin[3], float cell,
+                          const int32_t dims[3], uint64_t* keys_out, uint32_t* order_out, void* stream);
+
 /* Cell grid of the step (one scene): origin, cell size, dims. */
 int mps_get_grid(mps_handle* h, float origin[3], float* cell, int32_t dims[3]);
 

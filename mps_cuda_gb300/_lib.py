@@ -81,6 +81,8 @@ EXPORTS = {
     "mps_put_field": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int]),
     "mps_get_grid": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mps_profile_kernel": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
+    "mps_cell_sort_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
     "mps_create_batched": (C.c_int, [C.POINTER(Material), C.POINTER(Physics), C.POINTER(Config), C.c_int, C.c_int32,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "mps_set_batched": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
