@@ -81,6 +81,7 @@ typedef struct mps_config {
     int32_t volume_accumulate;   /* 1: reproduce the un-reset boundary volume (MPSSystem.cpp:237-238) */
     int32_t use_graph;           /* 1: whole step as one CUDA graph with device-side loops */
     int32_t block_size;          /* threads per block of the neighbour-sum kernels (64..256) */
+    int32_t stage;               /* 1: pressure passes stage neighbour data in shared memory (off by default: slower here) */
 } mps_config;
 
 /* Per-step statistics, written by the device at the end of each step. */

@@ -48,7 +48,7 @@ class Config(C.Structure):
                 ("cd_min_iter", C.c_int32), ("max_iter", C.c_int32), ("cg_tol", C.c_double), ("cg_max_iter", C.c_int32),
                 ("cg_factor", C.c_double), ("fixed_iters", C.c_int32), ("max_fluid_neighbors", C.c_int32),
                 ("max_boundary_neighbors", C.c_int32), ("volume_accumulate", C.c_int32), ("use_graph", C.c_int32),
-                ("block_size", C.c_int32)]
+                ("block_size", C.c_int32), ("stage", C.c_int32)]
 
 
 class Stats(C.Structure):

@@ -94,6 +94,8 @@ struct mps_handle {
     unsigned* nbr_f = nullptr;
     unsigned* nbr_b = nullptr;
     unsigned* cnt = nullptr;
+    unsigned short* nbr_l = nullptr;
+    Stage* stage = nullptr;
     float *rho = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
     float2* aux = nullptr;
     float4* color = nullptr;
@@ -139,7 +141,7 @@ void mps_handle::release() {
     drop_graphs();
     void** ptrs[] = {(void**)&pos[0], (void**)&pos[1], (void**)&vel[0], (void**)&vel[1], (void**)&ids[0],
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
-                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&rho,
+                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&nbr_l, (void**)&stage, (void**)&rho,
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol,
@@ -219,6 +221,9 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.nbr_f = h->nbr_f;
     d.nbr_b = h->nbr_b;
     d.cnt = h->cnt;
+    d.nbr_l = h->nbr_l;
+    d.stage = h->stage;
+    d.stage_on = h->cfg.stage ? 1 : 0;
     d.rho = h->rho;
     d.alpha = h->alpha;
     d.kappa = h->kappa;
@@ -331,6 +336,8 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->nbr_b, S * size_t(h->cfg.max_boundary_neighbors)));
     MPS_CUDA_TRY(dalloc(&h->cg_coef, S * size_t(h->cfg.max_fluid_neighbors)));
     MPS_CUDA_TRY(dalloc(&h->cnt, S));
+    MPS_CUDA_TRY(dalloc(&h->nbr_l, S * size_t(h->cfg.max_fluid_neighbors)));
+    MPS_CUDA_TRY(dalloc(&h->stage, S / 64 + 1));
     MPS_CUDA_TRY(cudaMemset(h->cnt, 0, S * sizeof(unsigned)));
     MPS_CUDA_TRY(dalloc(&h->rho, S));
     MPS_CUDA_TRY(dalloc(&h->alpha, S));
@@ -731,6 +738,7 @@ void mps_default_config(mps_config* c) {
     c->volume_accumulate = 0;
     c->use_graph = 1;
     c->block_size = 128;
+    c->stage = 0;
 }
 
 // SPHMaterial() + SetRadius(h): V = h^3 / 48 * 3.141592, mass = density * V

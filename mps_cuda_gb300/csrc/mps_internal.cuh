@@ -32,6 +32,16 @@ struct Scene {
     int bbegin, bend;               // boundary particles of this scene (sorted order)
 };
 
+// Shared-memory staging of a thread block's fluid neighbourhood.  The block's particles occupy
+// cells [kf, kl] (key order); every fluid neighbour lies in one of the nine key ranges
+// [kf + off - 1, kl + off + 1], off = dz*nx*ny + dy*nx for dz, dy in {-1, 0, 1}.  Those map to
+// nine slot ranges, merged here into disjoint sorted ranges lo[r]..hi[r] that are staged back to
+// back from base[r]; base[9] is the staged count.  Neighbour lists also carry the local index.
+constexpr int kStageCap = 2048;     // records per block (above this the block gathers from global)
+struct Stage {
+    int lo[9], hi[9], base[10];
+};
+
 // Device-resident solver state of one scene.
 struct SceneSolve {
     int active;       // still iterating
@@ -85,6 +95,9 @@ struct Dev {
     unsigned int* nbr_f;
     unsigned int* nbr_b;
     unsigned int* cnt;            // nf | nb << 16
+    unsigned short* nbr_l;        // block-local staged index of each fluid neighbour (like nbr_f)
+    Stage* stage;                 // staging layout per thread block of the pass kernels
+    int stage_on;                 // 1: pass kernels stage neighbour data in shared memory
     float* rho;
     float* alpha;
     float* kappa;

@@ -48,6 +48,28 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     return r;
 }
 
+// Block sums of two per-thread FP32 values: FP32 within a warp (32 terms), FP64 across warps.
+// GB300's FP64 rate is a small fraction of FP32, so per-thread products and shuffles stay FP32;
+// the result is valid in thread 0 only.
+template <int BS>
+__device__ __forceinline__ double2 block_sum2_f(float a, float b, double2* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(kFull, a, o);
+        b += __shfl_down_sync(kFull, b, o);
+    }
+    __syncthreads();
+    if (lane == 0) sh[warp] = make_double2(double(a), double(b));
+    __syncthreads();
+    double2 r = make_double2(0.0, 0.0);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int w = 0; w < BS / 32; ++w) { r.x += sh[w].x; r.y += sh[w].y; }
+    }
+    return r;
+}
+
 // Deterministic sum of this scene's per-block partials (component c of 2), run by one block.
 template <int BS>
 __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double* sh) {
@@ -141,14 +163,94 @@ __device__ __forceinline__ bool fluid_cell(const Dev& d, int slots, unsigned lon
     return e.x < e.y && e.x < unsigned(slots) && d.slot_key[e.x] == key;
 }
 
+// ------------------------------------------------------------------ shared-memory staging
+__device__ __forceinline__ int lower_bound_key(const unsigned long long* k, int a, int b, unsigned long long key) {
+    while (a < b) {
+        const int m = (a + b) >> 1;
+        if (k[m] < key) a = m + 1; else b = m;
+    }
+    return a;
+}
+__device__ __forceinline__ int upper_bound_key(const unsigned long long* k, int a, int b, unsigned long long key) {
+    while (a < b) {
+        const int m = (a + b) >> 1;
+        if (k[m] <= key) a = m + 1; else b = m;
+    }
+    return a;
+}
+
+// Computes the staging layout of this block (all threads call; result in st).  The nine key
+// ranges increase with (dz, dy) because ny >= 3, so merging them in order gives disjoint
+// sorted slot ranges.
+template <int BS>
+__device__ void compute_stage(const Dev& d, const Scene& sc, Stage& st) {
+    const int first = blockIdx.x * BS;
+    const int last = min(first + BS, sc.slot_begin + sc.n) - 1;
+    if (threadIdx.x < 9) {
+        int lo = sc.slot_begin, hi = sc.slot_begin;
+        if (last >= first) {
+            const int dz = int(threadIdx.x) / 3 - 1, dy = int(threadIdx.x) % 3 - 1;
+            const long long off = (long long)dz * sc.nx * sc.ny + (long long)dy * sc.nx;
+            const long long kb = (long long)sc.key_base;
+            const long long ke = kb + (long long)sc.nx * sc.ny * sc.nz - 1;
+            const long long klo = max((long long)d.slot_key[first] + off - 1, kb);
+            const long long khi = min((long long)d.slot_key[last] + off + 1, ke);
+            if (klo <= khi) {
+                const int e = sc.slot_begin + sc.n;
+                lo = lower_bound_key(d.slot_key, sc.slot_begin, e, (unsigned long long)klo);
+                hi = upper_bound_key(d.slot_key, lo, e, (unsigned long long)khi);
+            }
+        }
+        st.lo[threadIdx.x] = lo;
+        st.hi[threadIdx.x] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int e = st.lo[0], base = 0;
+        for (int r = 0; r < 9; ++r) {
+            const int lo = max(st.lo[r], e);
+            const int hi = max(st.hi[r], lo);
+            st.lo[r] = lo;
+            st.hi[r] = hi;
+            st.base[r] = base;
+            base += hi - lo;
+            e = hi;
+        }
+        st.base[9] = base;
+    }
+    __syncthreads();
+}
+
+// Block-local staged index of slot j (or -1 when j is outside the staged ranges).
+__device__ __forceinline__ int stage_index(const Stage& st, unsigned j) {
+    int loc = -1;
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        if (int(j) >= st.lo[r] && int(j) < st.hi[r]) loc = st.base[r] + (int(j) - st.lo[r]);
+    return loc;
+}
+
+// Copies this block's staging layout from global memory into shared memory.
+__device__ __forceinline__ void load_stage(const Dev& d, Stage& st) {
+    if (threadIdx.x < 28) reinterpret_cast<int*>(&st)[threadIdx.x] = reinterpret_cast<const int*>(&d.stage[blockIdx.x])[threadIdx.x];
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------ neighbour lists
 template <int BS>
 __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
     const Scene& sc = d.scenes[block_scene(d, BS)];
     __shared__ unsigned long long s_pf, s_pb;
-    if (threadIdx.x == 0) { s_pf = 0; s_pb = 0; }
-    __syncthreads();
+    __shared__ Stage st;
+    __shared__ int s_unmapped;
+    if (threadIdx.x == 0) { s_pf = 0; s_pb = 0; s_unmapped = 0; }
+    if (d.stage_on) {
+        compute_stage<BS>(d, sc, st);
+    } else {
+        __syncthreads();
+    }
+    const bool staged = d.stage_on && st.base[9] <= kStageCap;
     unsigned nf = 0, nb = 0;
     if (i < sc.slot_begin + sc.n) {
         const float4 xi = d.pos[i];
@@ -178,7 +280,16 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
                     const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
                     const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
                     if (d2 < __fmul_rn(hij, hij)) {
-                        if (nf < unsigned(p.cap_f)) d.nbr_f[size_t(nf) * stride + size_t(i)] = j; else over = true;
+                        if (nf < unsigned(p.cap_f)) {
+                            d.nbr_f[size_t(nf) * stride + size_t(i)] = j;
+                            if (staged) {
+                                const int loc = stage_index(st, j);
+                                if (loc < 0) s_unmapped = 1;
+                                d.nbr_l[size_t(nf) * stride + size_t(i)] = (unsigned short)(loc < 0 ? 0 : loc);
+                            }
+                        } else {
+                            over = true;
+                        }
                         nf++;
                     }
                 }
@@ -204,6 +315,13 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
     if (threadIdx.x == 0) {
         atomicAdd(&d.ctr->fluid_pairs, s_pf);
         atomicAdd(&d.ctr->boundary_pairs, s_pb);
+        // a block whose neighbours could not all be mapped (or that exceeds the capacity)
+        // gathers from global memory in the pass kernels
+        if (d.stage_on && (!staged || s_unmapped)) st.base[9] = kStageCap + 1;
+    }
+    if (d.stage_on) {
+        __syncthreads();
+        if (threadIdx.x < 28) reinterpret_cast<int*>(&d.stage[blockIdx.x])[threadIdx.x] = reinterpret_cast<const int*>(&st)[threadIdx.x];
     }
 }
 
@@ -334,6 +452,7 @@ __global__ void k_set_cond(Dev d, unsigned long long cond) {
 template <int BS>
 __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, unsigned long long cond, int use_cond) {
     __shared__ double sh[32];
+    __shared__ double2 sh2[BS / 32];
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
     const Scene& sc = d.scenes[s];
@@ -379,8 +498,8 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         d.kappa[i] = kap;
         d.delta[i] = delta;
     }
-    const double bsum = block_sum<BS>(double(err), sh);
-    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bsum;
+    const double2 bs2 = block_sum2_f<BS>(err, 0.0f, sh2);
+    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
     const double tot = scene_partial_sum<BS>(d, sc, 0, sh);
     if (threadIdx.x == 0) {
@@ -412,6 +531,24 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
     if (!profile && !d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
+    extern __shared__ float4 s_xk[];  // staged (x, y, z, kappa) of the block's neighbourhood
+    __shared__ Stage st;
+    bool staged = false;
+    if (d.stage_on) {
+        load_stage(d, st);
+        staged = st.base[9] <= kStageCap;
+        if (staged) {
+            for (int r = 0; r < 9; ++r) {
+                const int lo = st.lo[r], len = st.hi[r] - lo, b = st.base[r];
+                for (int t = threadIdx.x; t < len; t += BS) {
+                    float4 x = d.pos[lo + t];
+                    x.w = d.kappa[lo + t];
+                    s_xk[b + t] = x;
+                }
+            }
+            __syncthreads();
+        }
+    }
     if (i >= sc.slot_begin + sc.n) return;
     const size_t stride = size_t(p.slots);
     const float4 xi = d.pos[i];
@@ -420,15 +557,26 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
     const unsigned c = d.cnt[i];
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
-        const float4 xj = d.pos[j];
-        const float kj = d.kappa[j];
-        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const float invd = safe_rsqrt(d2);
-        const float g = (ki + kj) * kG(d2 * invd, invd, invh, p.cubic);
-        fx -= g * dx; fy -= g * dy; fz -= g * dz;
+    if (staged) {
+        for (int k = 0; k < nf; ++k) {
+            const float4 xj = s_xk[d.nbr_l[size_t(k) * stride + size_t(i)]];
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float invd = safe_rsqrt(d2);
+            const float g = (ki + xj.w) * kG(d2 * invd, invd, invh, p.cubic);
+            fx -= g * dx; fy -= g * dy; fz -= g * dz;
+        }
+    } else {
+        for (int k = 0; k < nf; ++k) {
+            const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
+            const float4 xj = d.pos[j];
+            const float kj = d.kappa[j];
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float invd = safe_rsqrt(d2);
+            const float g = (ki + kj) * kG(d2 * invd, invd, invh, p.cubic);
+            fx -= g * dx; fy -= g * dy; fz -= g * dz;
+        }
     }
     fx *= 0.5f * p.V; fy *= 0.5f * p.V; fz *= 0.5f * p.V;
     if (ki != 0.0f) {
@@ -592,22 +740,22 @@ __global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long long cond, int use_cond) {
     __shared__ double sh[32];
+    __shared__ double2 sh2[BS / 32];
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
-    double rr = 0.0, pap = 0.0;
+    float rr = 0.0f, pap = 0.0f;
     if (i < sc.slot_begin + sc.n) {
         const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor);
         d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
         const float4 r = d.cg_r[i];
         const float4 q = d.cg_p[i];
-        rr = double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
-        pap = double(q.x) * a.x + double(q.y) * a.y + double(q.z) * a.z;
+        rr = r.x * r.x + r.y * r.y + r.z * r.z;
+        pap = q.x * a.x + q.y * a.y + q.z * a.z;
     }
-    const double b0 = block_sum<BS>(rr, sh);
-    const double b1 = block_sum<BS>(pap, sh);
-    if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = b0; d.partial[2 * blockIdx.x + 1] = b1; }
+    const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
+    if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
     const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
     const double tpap = scene_partial_sum<BS>(d, sc, 1, sh);
@@ -635,11 +783,12 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p) {
     __shared__ double sh[32];
+    __shared__ double2 sh2[BS / 32];
     const int s = block_scene(d, BS);
     if (!d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
-    double rr = 0.0;
+    float rr = 0.0f;
     if (i < sc.slot_begin + sc.n) {
         const float a = float(d.solve[s].cg_alpha);
         float4 x = d.cg_x[i];
@@ -650,10 +799,10 @@ __global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p) {
         r.x -= a * ap.x; r.y -= a * ap.y; r.z -= a * ap.z;
         d.cg_x[i] = x;
         d.cg_r[i] = r;
-        rr = double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+        rr = r.x * r.x + r.y * r.y + r.z * r.z;
     }
-    const double b0 = block_sum<BS>(rr, sh);
-    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = b0;
+    const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
+    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
     if (!last_block_of_scene<BS>(d, s, sc)) return;
     const double t = scene_partial_sum<BS>(d, sc, 0, sh);
     if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
@@ -751,6 +900,13 @@ int nblocks_for(int n, int bs) { return (n + bs - 1) / bs; }
         else if ((bs) == 64) KERNEL<64><<<p.slots / 64, 64, 0, s>>>(__VA_ARGS__);            \
         else KERNEL<256><<<p.slots / 256, 256, 0, s>>>(__VA_ARGS__);                         \
     } while (0)
+// Same with `smem` bytes of dynamic shared memory (the staged neighbourhood).
+#define MPSG_BS_SWITCH_SMEM(bs, smem, KERNEL, ...)                                           \
+    do {                                                                                     \
+        if ((bs) == 128) KERNEL<128><<<p.slots / 128, 128, (smem), s>>>(__VA_ARGS__);        \
+        else if ((bs) == 64) KERNEL<64><<<p.slots / 64, 64, (smem), s>>>(__VA_ARGS__);       \
+        else KERNEL<256><<<p.slots / 256, 256, (smem), s>>>(__VA_ARGS__);                    \
+    } while (0)
 
 void launch_keys(const Dev& d, const Params& p, cudaStream_t s) {
     k_keys<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
@@ -779,10 +935,10 @@ void launch_pressure_A(const Dev& d, const Params& p, int mode, int bs, unsigned
 }
 void launch_pressure_B(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                        cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_pressure_B, d, p, 0, cond, use_cond, limit);
+    MPSG_BS_SWITCH_SMEM(bs, d.stage_on ? kStageCap * sizeof(float4) : 0, k_pressure_B, d, p, 0, cond, use_cond, limit);
 }
 void launch_pressure_B_profile(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_pressure_B, d, p, 1, 0ull, 0, 0);
+    MPSG_BS_SWITCH_SMEM(bs, d.stage_on ? kStageCap * sizeof(float4) : 0, k_pressure_B, d, p, 1, 0ull, 0, 0);
 }
 void launch_solver_finish(const Dev& d, const Params& p, int which, cudaStream_t s) {
     k_solver_finish<<<1, 256, 0, s>>>(d, p, which);
