@@ -54,7 +54,7 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms during the timed region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -68,7 +68,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -218,7 +218,7 @@ def run_ours(args, scene, rank, world, local_rank):
                    "parallelism": "replicas" if world > 1 else "single"},
         "iterations_per_step": {"df": iters[0] / args.steps, "cg": iters[1] / args.steps, "cd": iters[2] / args.steps},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+                     "frac": achieved / peak, "peak_source": src, "traffic": traffic, "traffic_source": "profiles/dram_traffic.json (ncu capture at 512k particles scaled to 1M)" if traffic else None,
                      "algorithmic_bytes_per_launch": algo, "ms_per_launch": per[dom],
                      "ms_per_launch_all": per},
         "step_roofline": {"algorithmic_bytes_per_step": step_algo,
@@ -252,7 +252,9 @@ def run_batched(args, scenes_list, rank, world, local_rank):
     mine = partition_scenes([s.n for s in scenes_list], world)[rank]
     local = [scenes_list[i] for i in mine]
     n_local = sum(s.n for s in local)
-    sim = BatchedSimulation(local, device=local_rank)
+    from mps_cuda_gb300.autotune import autotune
+    best, tuned = autotune(lambda **c: BatchedSimulation(local, device=local_rank, **c))
+    sim = BatchedSimulation(local, device=local_rank, **best)
     sim.step(args.warmup, stream)
     torch.cuda.synchronize(dev)
     if dist:
@@ -297,6 +299,8 @@ def run_batched(args, scenes_list, rank, world, local_rank):
                    "boundary_particles": sum(s.nb for s in scenes_list), "parallelism": "scenes split over ranks"},
         "per_scene_launches": {"value": per_value, "unit": UNIT, "ms_for_all_scenes_one_step": per_ms},
         "batched_over_per_scene": value / per_value,
+        "autotuned": {"best": best, "ms_per_step": {f"bs{c['block_size']}_d{c['sort_digit_bits']}": round(ms, 3)
+                                                    for ms, c in tuned}},
         "max_iterations": {"df": int(its[:, 0].max()), "cg": int(its[:, 1].max()), "cd": int(its[:, 2].max())},
         "clocks": clk.summary(),
     }

@@ -82,6 +82,7 @@ typedef struct mps_config {
     int32_t use_graph;           /* 1: whole step as one CUDA graph with device-side loops */
     int32_t block_size;          /* threads per block of the neighbour-sum kernels (64..256) */
     int32_t stage;               /* 1: pressure passes stage neighbour data in shared memory (off by default: slower here) */
+    int32_t sort_digit_bits;     /* radix digit width of the cell sort (1..8) */
 } mps_config;
 
 /* Per-step statistics, written by the device at the end of each step. */
@@ -217,6 +218,19 @@ int64_t mps_gen_box_walls(const double lo[3], const double hi[3], double spacing
                           int32_t open_mask, float* pos4);
 /* Sphere surface sampled at about spacing (Fibonacci lattice).  Returns count; pos4 may be NULL. */
 int64_t mps_gen_sphere(const double center[3], double R, double spacing, double radius, float* pos4);
+
+/* ---- Mesh boundaries (scene set-up; replaces MeshObject::LoadMesh + ParticleSampling) ---- */
+/* Reads "v x y z" and "f a b c ..." records of an OBJ file (1-based indices, polygons fanned into
+ * triangles) and, when center/size are given, fits the mesh's bounding box to that box per axis
+ * (MPSMeshObject.cu:58-103).  Two-call form: pass NULL arrays to get the counts. */
+int mps_mesh_load_obj(const char* path, const double center[3], const double size[3], int64_t* nverts,
+                      int64_t* nfaces, double* verts3, uint32_t* faces3);
+/* Boundary particles on a triangle mesh, sampled on the GPU as the reference's ParticleSampling
+ * (MPSParticleSamplingUtil.cu:42-133): each face writes the vertices and edges it owns and its
+ * scanlines at spacing mesh_radius / 2; particle radius mesh_radius / 4.  Returns the count (or a
+ * negative MPS_E_* code); pos4 NULL = count only; face_id optional. */
+int64_t mps_mesh_sample(const double* verts3, int64_t nv, const uint32_t* faces3, int64_t nf,
+                        double mesh_radius, float* pos4, uint32_t* face_id);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

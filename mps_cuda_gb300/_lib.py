@@ -48,7 +48,7 @@ class Config(C.Structure):
                 ("cd_min_iter", C.c_int32), ("max_iter", C.c_int32), ("cg_tol", C.c_double), ("cg_max_iter", C.c_int32),
                 ("cg_factor", C.c_double), ("fixed_iters", C.c_int32), ("max_fluid_neighbors", C.c_int32),
                 ("max_boundary_neighbors", C.c_int32), ("volume_accumulate", C.c_int32), ("use_graph", C.c_int32),
-                ("block_size", C.c_int32), ("stage", C.c_int32)]
+                ("block_size", C.c_int32), ("stage", C.c_int32), ("sort_digit_bits", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -92,6 +92,10 @@ EXPORTS = {
                                 C.c_double, C.c_uint64, C.c_void_p, C.c_void_p]),
     "mps_gen_box_walls": (C.c_int64, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
     "mps_gen_sphere": (C.c_int64, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_void_p]),
+    "mps_mesh_load_obj": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.c_void_p, C.c_void_p]),
+    "mps_mesh_sample": (C.c_int64, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p,
+                                    C.c_void_p]),
 }
 
 _lib = None

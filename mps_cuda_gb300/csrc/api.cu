@@ -429,7 +429,7 @@ int phase_sort(mps_handle* h, cudaStream_t s) {
     const Dev d = make_dev(h, 1 - h->cur);
     launch_keys(d, p, s);
     MPS_CUDA_TRY(radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n),
-                                  h->key_bits, 8, s));
+                                  h->key_bits, h->cfg.sort_digit_bits, s));
     launch_reorder(d, p, int(h->n), s);
     h->cur = 1 - h->cur;
     return MPS_OK;
@@ -579,7 +579,7 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         // sort + neighbours + density/alpha + gravity, then DF loop set-up
         MPS_CAP_TRY(seg_begin(c));
         launch_keys(d, p, c.s);
-        MPS_CAP_TRY(radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, 8, c.s));
+        MPS_CAP_TRY(radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, h->cfg.sort_digit_bits, c.s));
         launch_reorder(d, p, int(h->n), c.s);
         MPS_CAP_TRY(cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 2 * sizeof(unsigned long long), c.s));
         launch_build_nbrs(d, p, bs, c.s);
@@ -739,6 +739,7 @@ void mps_default_config(mps_config* c) {
     c->use_graph = 1;
     c->block_size = 128;
     c->stage = 0;
+    c->sort_digit_bits = 8;
 }
 
 // SPHMaterial() + SetRadius(h): V = h^3 / 48 * 3.141592, mass = density * V
@@ -773,6 +774,7 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (h->cfg.max_boundary_neighbors <= 0 || h->cfg.max_boundary_neighbors > 65535) h->cfg.max_boundary_neighbors = 64;
     if (h->cfg.max_iter <= 0) h->cfg.max_iter = 100;
     if (h->cfg.cg_max_iter <= 0) h->cfg.cg_max_iter = 100;
+    if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;
     *out = h;
     return MPS_OK;
 }
@@ -1119,7 +1121,7 @@ int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream
                 // re-sort the current order in place: keys from buffer cur, reorder into the other
                 const Dev ds = make_dev(h, 1 - h->cur);
                 launch_keys(ds, p, s);
-                radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, 8, s);
+                radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, h->cfg.sort_digit_bits, s);
                 launch_reorder(ds, p, int(h->n), s);
                 h->cur = 1 - h->cur;
                 break;

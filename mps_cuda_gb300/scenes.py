@@ -87,6 +87,35 @@ def gen_sphere(center, R, spacing, radius):
     return out
 
 
+def load_obj(path: str, center=None, size=None) -> tuple[np.ndarray, np.ndarray]:
+    """OBJ mesh -> (vertices (V, 3) float64, faces (F, 3) uint32), optionally fitted to a box."""
+    lib = L.load()
+    nv, nf = C.c_int64(), C.c_int64()
+    c = None if center is None else (C.c_double * 3)(*center)
+    s = None if size is None else (C.c_double * 3)(*size)
+    L.check(lib.mps_mesh_load_obj(str(path).encode(), c, s, C.byref(nv), C.byref(nf), None, None))
+    V = np.zeros((nv.value, 3), np.float64)
+    F = np.zeros((nf.value, 3), np.uint32)
+    L.check(lib.mps_mesh_load_obj(str(path).encode(), c, s, C.byref(nv), C.byref(nf), _ptr(V), _ptr(F)))
+    return V, F
+
+
+def sample_mesh(V: np.ndarray, F: np.ndarray, mesh_radius: float, with_faces: bool = False):
+    """Boundary particles (N, 4) float32 on a triangle mesh (GPU), as the reference samples its obstacles."""
+    lib = L.load()
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.uint32)
+    n = lib.mps_mesh_sample(_ptr(V), V.shape[0], _ptr(F), F.shape[0], mesh_radius, None, None)
+    if n < 0:
+        L.check(int(n))
+    out = np.zeros((n, 4), np.float32)
+    fid = np.zeros(n, np.uint32)
+    m = lib.mps_mesh_sample(_ptr(V), V.shape[0], _ptr(F), F.shape[0], mesh_radius, _ptr(out), _ptr(fid))
+    if m < 0:
+        L.check(int(m))
+    return (out, fid) if with_faces else out
+
+
 def physical_material(spacing: float, rho0: float = 1000.0, visc: float = 0.01, sigma: float = 0.05,
                       xsph: float = 0.1, radius: float | None = None) -> dict:
     V = spacing ** 3

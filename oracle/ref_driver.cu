@@ -23,6 +23,12 @@
 #include "MPS_Object/MPSUniformDef.h"
 #include "MPS_Computer/MPSAdvectUtil.h"
 #include "MPS_Computer/MPSSPHUtil.h"
+#include "MPS_Object/MPSMeshObject.cuh"
+#include "MPS_Computer/MPSParticleSamplingUtil.cuh"
+#include <thrust/scan.h>
+#include <thrust/sort.h>
+#include <thrust/transform.h>
+#include <algorithm>
 
 #define REF_API extern "C" __attribute__((visibility("default")))
 
@@ -277,6 +283,71 @@ REF_API long long ref_get(void* hp, const char* name, void* out) {
         return (long long)idx[rows];
     }
     return -1;
+}
+
+// The reference's mesh path on given vertices/faces: adjacency and R-triangle ownership as
+// MeshObject::buildAdjacency does (MPSMeshObject.cu:172-214), then ParticleSampling
+// (MPSParticleSamplingUtil.cu:42-133).  Writes up to cap positions (x, y, z) and returns the
+// sample count (or -1 on a CUDA error).
+REF_API long long ref_sample_mesh(const double* verts, long long nv, const unsigned* faces, long long nf,
+                                  double mesh_radius, double* out_pos3, long long cap) {
+    thrust::device_vector<glm::uvec3> d_face(reinterpret_cast<const glm::uvec3*>(faces),
+                                             reinterpret_cast<const glm::uvec3*>(faces) + nf);
+    thrust::device_vector<REAL3> d_pos(reinterpret_cast<const REAL3*>(verts), reinterpret_cast<const REAL3*>(verts) + nv);
+    const unsigned nb = 256u;
+    const unsigned grid = unsigned((nf + nb - 1) / nb);
+    thrust::device_vector<uint32_t> nbFacesID(size_t(nv) + 1, 0u);
+    ComputeNbFacesSize_kernel<<<grid, nb>>>(thrust::raw_pointer_cast(d_face.data()), size_t(nf),
+                                            thrust::raw_pointer_cast(nbFacesID.data()));
+    thrust::exclusive_scan(nbFacesID.begin(), nbFacesID.end(), nbFacesID.begin());
+    thrust::device_vector<uint32_t> nbFacesIdx = nbFacesID;
+    const uint32_t total = nbFacesID.back();
+    thrust::device_vector<uint2> vertexID(total);
+    thrust::device_vector<uint32_t> nbFaces(total);
+    ComputeNbFaces_kernel<<<grid, nb>>>(thrust::raw_pointer_cast(d_face.data()), size_t(nf),
+                                        thrust::raw_pointer_cast(vertexID.data()),
+                                        thrust::raw_pointer_cast(nbFacesID.data()));
+    thrust::sort(vertexID.begin(), vertexID.end(), mcuda::util::SortUint2CMP());
+    thrust::transform(vertexID.begin(), vertexID.end(), nbFaces.begin(), mcuda::util::TransformUint2CMP());
+    thrust::device_vector<uint32_t> rTri(nf, 0u);
+    RTriangleBuild_kernel<<<grid, nb>>>(thrust::raw_pointer_cast(d_face.data()), size_t(nf),
+                                        thrust::raw_pointer_cast(nbFaces.data()),
+                                        thrust::raw_pointer_cast(nbFacesIdx.data()),
+                                        thrust::raw_pointer_cast(rTri.data()));
+    mps::MeshMaterialParam mat{};
+    mat.radius = mesh_radius;
+    mat.frontColor = glm::fvec4{0.0f, 0.0f, 0.0f, 1.0f};
+    thrust::device_vector<uint32_t> sampSize(nf, 0u), shortEdge(nf, 0u), prevIdx(size_t(nf) + 1, 0u),
+        currIdx(size_t(nf) + 1, 0u);
+    thrust::device_vector<bool> isGen(nf, false), applied(1, false);
+    ComputeSamplingNum_kernel<<<grid, nb>>>(mat, thrust::raw_pointer_cast(d_face.data()),
+                                            thrust::raw_pointer_cast(d_pos.data()), thrust::raw_pointer_cast(rTri.data()),
+                                            thrust::raw_pointer_cast(sampSize.data()),
+                                            thrust::raw_pointer_cast(shortEdge.data()), size_t(nf),
+                                            thrust::raw_pointer_cast(prevIdx.data()),
+                                            thrust::raw_pointer_cast(currIdx.data()),
+                                            thrust::raw_pointer_cast(isGen.data()),
+                                            thrust::raw_pointer_cast(applied.data()));
+    thrust::exclusive_scan(prevIdx.begin(), prevIdx.end(), prevIdx.begin());
+    thrust::exclusive_scan(currIdx.begin(), currIdx.end(), currIdx.begin());
+    const uint32_t count = currIdx.back();
+    thrust::device_vector<uint32_t> faceID(count);
+    thrust::device_vector<REAL2> bcc(count);
+    thrust::device_vector<REAL3> pos(count);
+    thrust::device_vector<REAL> rad(count);
+    thrust::device_vector<glm::fvec4> col(count);
+    GenerateBoundaryParticle_kernel<<<grid, nb>>>(
+        mat, thrust::raw_pointer_cast(d_face.data()), thrust::raw_pointer_cast(d_pos.data()),
+        thrust::raw_pointer_cast(rTri.data()), thrust::raw_pointer_cast(shortEdge.data()), size_t(nf),
+        thrust::raw_pointer_cast(faceID.data()), thrust::raw_pointer_cast(bcc.data()), thrust::raw_pointer_cast(pos.data()),
+        thrust::raw_pointer_cast(rad.data()), thrust::raw_pointer_cast(col.data()), nullptr, nullptr, nullptr, nullptr,
+        nullptr, thrust::raw_pointer_cast(prevIdx.data()), thrust::raw_pointer_cast(currIdx.data()),
+        thrust::raw_pointer_cast(isGen.data()));
+    if (cudaDeviceSynchronize() != cudaSuccess) return -1;
+    if (out_pos3 && count > 0)
+        cudaMemcpy(out_pos3, thrust::raw_pointer_cast(pos.data()), size_t(std::min<long long>(count, cap)) * sizeof(REAL3),
+                   cudaMemcpyDeviceToHost);
+    return (long long)count;
 }
 
 REF_API int ref_put(void* hp, const char* name, const double* in, long long count) {

@@ -46,8 +46,23 @@ def load(variant: str = "shipped") -> C.CDLL:
     lib.ref_get.restype = C.c_longlong
     lib.ref_get.argtypes = [vp, C.c_char_p, vp]
     lib.ref_put.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+    lib.ref_sample_mesh.restype = C.c_longlong
+    lib.ref_sample_mesh.argtypes = [vp, C.c_longlong, vp, C.c_longlong, C.c_double, vp, C.c_longlong]
     _libs[variant] = lib
     return lib
+
+
+def sample_mesh(V: np.ndarray, F: np.ndarray, mesh_radius: float, variant: str = "shipped") -> np.ndarray:
+    """The reference's own ParticleSampling on a mesh: (N, 3) float64 positions."""
+    lib = load(variant)
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.uint32)
+    n = lib.ref_sample_mesh(_p(V), V.shape[0], _p(F), F.shape[0], mesh_radius, None, 0)
+    if n < 0:
+        raise RuntimeError("reference mesh sampling failed")
+    out = np.zeros((n, 3), np.float64)
+    lib.ref_sample_mesh(_p(V), V.shape[0], _p(F), F.shape[0], mesh_radius, _p(out), n)
+    return out
 
 
 def _p(a):
