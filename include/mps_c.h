@@ -83,7 +83,16 @@ typedef struct mps_config {
     int32_t block_size;          /* threads per block of the neighbour-sum kernels (64..256) */
     int32_t stage;               /* 1: pressure passes stage neighbour data in shared memory (off by default: slower here) */
     int32_t sort_digit_bits;     /* radix digit width of the cell sort (1..8) */
+    int32_t visc_solver;         /* mps_visc_solver: implicit viscosity/surface-tension solve */
 } mps_config;
+
+/* MPS_VISC_CG: the reference's CGSolver (MPSSolver.cuh:12-73).  MPS_VISC_JACOBI: point-Jacobi
+ * sweeps on the same system, the alternative of the reference's legacy Jacobi viscosity
+ * (MPSSPHNonPressureUtil.cuh:90-195, commented out there).  The CG's converged point satisfies
+ * (A_0 + f I) x = b + f x0 (f = cg_factor, x0 = pre-solve velocity); Jacobi iterates
+ * x += D^-1 (b + f x0 - (A_0 + f I) x), D = diag(A_0 + f I), from x0, stopping when the residual's
+ * r.r < cg_tol (at most cg_max_iter sweeps) or after fixed_iters sweeps. */
+enum mps_visc_solver { MPS_VISC_CG = 0, MPS_VISC_JACOBI = 1 };
 
 /* Per-step statistics, written by the device at the end of each step. */
 typedef struct mps_stats {
@@ -231,6 +240,24 @@ int mps_mesh_load_obj(const char* path, const double center[3], const double siz
  * negative MPS_E_* code); pos4 NULL = count only; face_id optional. */
 int64_t mps_mesh_sample(const double* verts3, int64_t nv, const uint32_t* faces3, int64_t nf,
                         double mesh_radius, float* pos4, uint32_t* face_id);
+
+/* ---- Adjoint (reverse-mode gradient of a rollout) ----
+ * No counterpart in the reference, which has no differentiation.  Requirements: fixed_iters > 0
+ * (every solve runs a fixed count), visc_solver = MPS_VISC_JACOBI, volume_accumulate = 0.
+ * mps_adjoint_forward runs nsteps steps from the current state exactly like mps_step and keeps
+ * a checkpoint (slot-order state) every checkpoint_every steps on the device.
+ * mps_adjoint_backward takes the cotangents of the final state (host, particle-ID order, 4
+ * floats per particle, the 4th ignored; either may be NULL = zero) and returns, per particle in
+ * ID order, d/d(initial position) and d/d(initial velocity) (4 floats each, 4th = 0), and per
+ * scene d/d(viscosity) and d/d(surface_tension) (2 doubles per scene).  Steps between
+ * checkpoints are recomputed with neighbour lists rebuilt; each step's solves are reversed as
+ * transposed Jacobi sweeps of the same fixed count.  The handle is left at the final state.
+ * The neighbour lists are assumed symmetric (MPS_E_STATE otherwise). */
+int mps_adjoint_forward(mps_handle* h, int32_t nsteps, int32_t checkpoint_every, void* stream);
+int mps_adjoint_backward(mps_handle* h, const float* g_pos4, const float* g_vel4, float* g_pos0,
+                         float* g_vel0, double* g_param2, void* stream);
+/* Device bytes the adjoint holds for the current layout (checkpoints + one step's tape). */
+int64_t mps_adjoint_memory(mps_handle* h, int32_t nsteps, int32_t checkpoint_every);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -26,6 +26,7 @@ ERRORS = {
 PHASE_SORT, PHASE_NEIGHBORS, PHASE_BVOLUME, PHASE_DENSITY_ALPHA, PHASE_DF, PHASE_VISCST, PHASE_CD, PHASE_ADVECT = range(8)
 KERNEL_POLY6_SPIKY, KERNEL_CUBIC_SPLINE = 0, 1
 K_PRESSURE_A, K_PRESSURE_B, K_CG_AP, K_DENSITY_ALPHA, K_BUILD_NBRS, K_SORT = range(6)
+VISC_CG, VISC_JACOBI = 0, 1
 
 
 class MpsError(RuntimeError):
@@ -48,7 +49,8 @@ class Config(C.Structure):
                 ("cd_min_iter", C.c_int32), ("max_iter", C.c_int32), ("cg_tol", C.c_double), ("cg_max_iter", C.c_int32),
                 ("cg_factor", C.c_double), ("fixed_iters", C.c_int32), ("max_fluid_neighbors", C.c_int32),
                 ("max_boundary_neighbors", C.c_int32), ("volume_accumulate", C.c_int32), ("use_graph", C.c_int32),
-                ("block_size", C.c_int32), ("stage", C.c_int32), ("sort_digit_bits", C.c_int32)]
+                ("block_size", C.c_int32), ("stage", C.c_int32), ("sort_digit_bits", C.c_int32),
+                ("visc_solver", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -96,6 +98,10 @@ EXPORTS = {
                                     C.c_void_p, C.c_void_p]),
     "mps_mesh_sample": (C.c_int64, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p,
                                     C.c_void_p]),
+    "mps_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "mps_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    "mps_adjoint_memory": (C.c_int64, [C.c_void_p, C.c_int32, C.c_int32]),
 }
 
 _lib = None

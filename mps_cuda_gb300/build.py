@@ -20,7 +20,7 @@ BUILD = HERE / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
-SOURCES = ["sort.cu", "sph.cu", "api.cu", "noalloc.cu", "mesh.cu", "scene.cpp"]
+SOURCES = ["sort.cu", "sph.cu", "api.cu", "noalloc.cu", "mesh.cu", "adjoint.cu", "scene.cpp"]
 
 
 def nvcc() -> str:

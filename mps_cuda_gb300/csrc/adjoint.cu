@@ -1,0 +1,1048 @@
+// Reverse-mode gradient of a DFSPH rollout (the adjoint form of the step).  The reference has no
+// differentiation; this file adds it on top of the same step kernels (sph.cu), which it re-runs
+// with recording hooks.
+//
+// Differentiated step (fixed iteration counts K, Jacobi viscosity/surface-tension solve):
+//   rho_i   = rho0 (V W_ii + V sum_j W_ij + sum_b Vb W_ib)                     (density)
+//   alpha_i = 1 / (|V sum_j G_ij x_ij + sum_b Vb G_ib x_ib|^2 + sum_j |V G_ij x_ij|^2)
+//   v      += dt g
+//   K x DF:  delta_i = V sum_j G_ij x_ij.(u_i - u_j) + sum_b Vb G_ib x_ib.u_i,
+//            kappa_i = max(0, min(dt delta_i, rho_i/rho0 + dt delta_i - 0.8)) alpha_i / dt^2,
+//            u_i    += -dt [0.5 V sum_j (kappa_i + kappa_j) G_ij x_ij + 0.5 kappa_i sum_b Vb G_ib x_ib]
+//   viscosity + surface tension + XSPH: coefficients c_ij, cv_ij, b_i from (x, v, rho, st factor)
+//            (k_cg_b), then K Jacobi sweeps q += D^-1 (b + f x0 - (A_0 + f I) q) from q = x0 = v
+//   K x CD:  as DF with kappa_i = max(0, rho_i/rho0 + dt delta_i - 1) alpha_i / dt^2
+//   collision (per axis: v, -0.4 v or 0) and x += dt v.
+// Neighbour sets are piecewise constant in x (no derivative).  Every pair term's reverse is
+// evaluated in gather form: particle i adds the derivatives of the terms it owns (pairs (i, j) of
+// its list) and of the terms its neighbours own (pairs (j, i), found through the reverse index
+// rev[k][i] = position of i in j's list), so each cotangent is written by one thread and the
+// result is deterministic.  The Jacobi solve reverses exactly as K transposed sweeps
+// y = qbar / D, qbar -= (A_0 + f I)^T y.
+//
+// Memory: checkpoints of the slot-order state every `every` steps, the start states of one
+// segment, and one step's tape (K + 1 velocity fields per pressure solve, K + 1 Jacobi iterates,
+// stiffness and branch codes), plus per-pair cotangents of the solve's coefficients.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "handle.cuh"
+#include "mps_c.h"
+#include "mps_internal.cuh"
+
+namespace mpsg {
+
+struct AdjointStore {
+    int nsteps = 0, every = 0;       // the recorded forward
+    int K = 0, ncp_cap = 0, every_cap = 0;   // capacities of the buffers
+    int slots = 0, cap = 0, nscenes = 0;
+    int64_t n = 0;
+    size_t bytes = 0;
+    bool ready = false;              // a forward was recorded
+    // checkpoints (slot order of the buffer that was current) and the final state
+    float4 *cp_pos = nullptr, *cp_vel = nullptr;
+    unsigned* cp_ids = nullptr;
+    std::vector<int> cp_cur;
+    float4 *fin_pos = nullptr, *fin_vel = nullptr;
+    unsigned* fin_ids = nullptr;
+    int fin_cur = 0;
+    int64_t fin_steps = 0;
+    // start states of the steps of one segment
+    float4 *seg_pos = nullptr, *seg_vel = nullptr;
+    unsigned* seg_ids = nullptr;
+    std::vector<int> seg_cur;
+    // one step's tape
+    float4 *t_udf = nullptr, *t_ucd = nullptr, *t_q = nullptr, *t_x = nullptr;
+    float *t_kdf = nullptr, *t_kcd = nullptr;
+    unsigned char *t_cdf = nullptr, *t_ccd = nullptr, *t_adv = nullptr;
+    // cotangents
+    float4 *gx = nullptr, *gv = nullptr, *gx_id = nullptr, *gv_id = nullptr;
+    float4 *qbar0 = nullptr, *qbar1 = nullptr, *bbar = nullptr, *Dbar = nullptr, *gg = nullptr;
+    float *grho = nullptr, *galpha = nullptr, *gdelta = nullptr, *gsf = nullptr, *gsig = nullptr, *gmu = nullptr;
+    float2* pc = nullptr;            // per pair (cbar, cvbar), interleaved like nbr_f
+    float4* px = nullptr;            // per pair explicit x_ij cotangent
+    unsigned char* rev = nullptr;    // per pair: position of i in the neighbour's list
+    double* gparam = nullptr;        // 2 per scene
+    int* flag = nullptr;             // bit0: asymmetric neighbour lists
+    StepCounters* ctr_save = nullptr;
+
+    void free_all() {
+        void* ptrs[] = {cp_pos, cp_vel, cp_ids, fin_pos, fin_vel, fin_ids, seg_pos, seg_vel, seg_ids, t_udf, t_ucd,
+                        t_q, t_x, t_kdf, t_kcd, t_cdf, t_ccd, t_adv, gx, gv, gx_id, gv_id, qbar0, qbar1, bbar,
+                        Dbar, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+        *this = AdjointStore{};
+    }
+};
+
+namespace {
+
+constexpr int kAB = 128;   // threads per block of the adjoint kernels (divides the slot padding)
+
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3& operator+=(float3& a, float3 b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
+__device__ __forceinline__ float3& operator-=(float3& a, float3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; return a; }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 mul3(float3 a, float3 b) { return make_float3(a.x * b.x, a.y * b.y, a.z * b.z); }
+
+// Kernel values and radial derivatives at distance r: W, dW/dr, G (grad W = G x), dG/dr.
+// Same piecewise forms as kW / kG (MPSSPHKernel.cuh:28-65), differentiated per piece.
+struct KD {
+    float W, dW, G, dG;
+};
+__device__ __forceinline__ KD kern_d(float r, float invh, int cubic) {
+    KD k{0.0f, 0.0f, 0.0f, 0.0f};
+    const float q = r * invh;
+    if (q >= 1.0f) return k;
+    const float ih2 = invh * invh, ih4 = ih2 * ih2;
+    if (cubic) {
+        if (q > 0.5f) {
+            const float t = 1.0f - q;
+            const float ir = 1.0f / r;
+            k.W = 2.0f * KC::cw * t * t * t * ih2 * invh;
+            k.dW = -6.0f * KC::cw * t * t * ih4;
+            k.G = -KC::cg * t * t * ih4 * ir;
+            k.dG = KC::cg * ih4 * t * ir * (2.0f * invh + t * ir);
+        } else {
+            k.W = KC::cw * ih2 * invh * ((6.0f * q - 6.0f) * q * q + 1.0f);
+            k.dW = KC::cw * ih4 * (18.0f * q * q - 12.0f * q);
+            k.G = (q < 1.0e-20f) ? 0.0f : KC::cg * ih4 * invh * (3.0f * q - 2.0f);
+            k.dG = (q < 1.0e-20f) ? 0.0f : 3.0f * KC::cg * ih4 * ih2;
+        }
+        return k;
+    }
+    const float s = 1.0f - q * q;
+    k.W = KC::w * s * s * s * ih2 * invh;
+    k.dW = -6.0f * KC::w * q * s * s * ih4;
+    if (q >= 1.0e-20f) {
+        const float t = 1.0f - q;
+        const float ir = 1.0f / r;
+        k.G = -KC::g * t * t * ih4 * ir;
+        k.dG = KC::g * ih4 * t * ir * (2.0f * invh + t * ir);
+    }
+    return k;
+}
+// Surface-tension kernels (MPSSPHKernel.cuh:67-84): STW, dSTW/dr, STG, dSTG/dr.
+__device__ __forceinline__ KD kern_st(float r, float invh) {
+    KD k{0.0f, 0.0f, 0.0f, 0.0f};
+    const float q = r * invh;
+    if (q >= 1.0f) return k;
+    const float ih2 = invh * invh, ih4 = ih2 * ih2;
+    const float qq = fmaxf(q, 0.5f);
+    const float tt = 1.0f - qq;
+    k.W = KC::stw * tt * tt * tt * ih2 * invh;
+    if (q > 0.5f) {
+        const float t = 1.0f - q;
+        const float ir = 1.0f / r;
+        k.dW = -3.0f * KC::stw * t * t * ih4;
+        k.G = -KC::stg * t * t * ih4 * ir;
+        k.dG = KC::stg * ih4 * t * ir * (2.0f * invh + t * ir);
+    }
+    return k;
+}
+
+__device__ __forceinline__ bool slot_live(const Dev& d, int i, int& s) {
+    s = d.chunk_scene[i / kChunk];
+    const Scene& sc = d.scenes[s];
+    return i < sc.slot_begin + sc.n;
+}
+
+// ------------------------------------------------------------------ bookkeeping kernels
+__global__ void k_adj_rev(Dev d, Params p, unsigned char* rev, int* flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const int nf = int(d.cnt[i] & 0xffffu);
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
+        const int nj = int(d.cnt[j] & 0xffffu);
+        int r = 255;
+        for (int t = 0; t < nj; ++t)
+            if (d.nbr_f[size_t(t) * S + j] == unsigned(i)) { r = t; break; }
+        if (r == 255) atomicOr(flag, 1);
+        rev[size_t(k) * S + size_t(i)] = (unsigned char)r;
+    }
+}
+
+// ID order -> slot order of the current layout, and per-step accumulators reset.
+__global__ void k_adj_gather(Dev d, Params p, const float4* gx_id, const float4* gv_id, float4* gx, float4* gv,
+                             float* grho, float* galpha) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    grho[i] = 0.0f;
+    galpha[i] = 0.0f;
+    if (!slot_live(d, i, s)) {
+        gx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        gv[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const unsigned id = d.ids[i];
+    gx[i] = gx_id[id];
+    gv[i] = gv_id[id];
+}
+
+__global__ void k_adj_scatter(Dev d, Params p, const float4* gx, const float4* gv, float4* gx_id, float4* gv_id) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const unsigned id = d.ids[i];
+    float4 a = gx[i], b = gv[i];
+    a.w = 0.0f;
+    b.w = 0.0f;
+    gx_id[id] = a;
+    gv_id[id] = b;
+}
+
+// ------------------------------------------------------------------ collision + position
+// x' = x + dt v_c, v_c = s v per axis (s = 1, -0.4 or 0 by the recorded branch).
+__global__ void k_adj_advect(Dev d, Params p, const unsigned char* code, float4* gx, float4* gv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const float4 X = gx[i];
+    float4 V = gv[i];
+    const unsigned c = code[i];
+    auto sc = [](unsigned b) { return b == 0u ? 1.0f : (b == 1u ? -0.4f : 0.0f); };
+    V.x = sc(c & 3u) * (V.x + p.dt * X.x);
+    V.y = sc((c >> 2) & 3u) * (V.y + p.dt * X.y);
+    V.z = sc((c >> 4) & 3u) * (V.z + p.dt * X.z);
+    gv[i] = V;
+}
+
+// ------------------------------------------------------------------ pressure iteration
+// First half of one DF/CD iteration's reverse: abar = dt ubar' (massive particles), the
+// stiffness cotangent kbar_i, its chain through the clamp / min branch into delta, rho, alpha,
+// and the x cotangent of the pressure-force terms.
+__global__ void __launch_bounds__(kAB) k_adj_pA(Dev d, Params p, const float4* X, const float* kap,
+                                                 const unsigned char* code, const float4* gv, float* gdelta,
+                                                 float* grho, float* galpha, float4* gx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float invhi = 1.0f / xi.w;
+    const float ki = kap[i];
+    const float4 gvi = gv[i];
+    const float4 vi = d.vel[i];   // mass in w (unchanged through the step)
+    const float3 ai = vi.w > 1.0e-10f ? p.dt * f3(gvi) : make_float3(0.f, 0.f, 0.f);
+    const unsigned c = d.cnt[i];
+    const int nf = int(c & 0xffffu), nb = int(c >> 16);
+    float kbar = 0.0f;
+    float3 xa = make_float3(0.f, 0.f, 0.f);
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
+        const float4 xj = X[j];
+        const float kj = kap[j];
+        const float3 aj = d.vel[j].w > 1.0e-10f ? p.dt * f3(gv[j]) : make_float3(0.f, 0.f, 0.f);
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD Ki = kern_d(r, invhi, p.cubic);
+        const KD Kj = xj.w == xi.w ? Ki : kern_d(r, 1.0f / xj.w, p.cubic);
+        const float aie = dot3(ai, e), aje = dot3(aj, e);
+        kbar += -0.5f * p.V * (Ki.G * aie - Kj.G * aje);
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        const float3 ti = Ki.G * ai + (Ki.dG * ir * aie) * e;
+        const float3 tj = Kj.G * aj + (Kj.dG * ir * aje) * e;
+        xa += (-0.5f * p.V * (ki + kj)) * (ti - tj);
+    }
+    for (int k = 0; k < nb; ++k) {
+        const unsigned b = d.nbr_b[size_t(k) * S + size_t(i)];
+        const float4 xb = d.bpos[b];
+        const float vb = d.bvol[b];
+        const float3 e = make_float3(xi.x - xb.x, xi.y - xb.y, xi.z - xb.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD K = kern_d(r, invhi, p.cubic);
+        const float aie = dot3(ai, e);
+        kbar += -0.5f * vb * K.G * aie;
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        xa += (-0.5f * ki * vb) * (K.G * ai + (K.dG * ir * aie) * e);
+    }
+    float4 g = gx[i];
+    g.x += xa.x; g.y += xa.y; g.z += xa.z;
+    gx[i] = g;
+    const unsigned char cd = code[i];
+    float gd = 0.0f;
+    if (cd != 0) {
+        const float al = d.alpha[i];
+        const float kb = kbar * al * (p.inv_dt * p.inv_dt);
+        if (al > 0.0f) galpha[i] += kbar * ki / al;
+        gd = kb * p.dt;
+        if (cd == 2) grho[i] += kb * p.inv_rho0;
+    }
+    gdelta[i] = gd;
+}
+
+// Second half: the delta terms' cotangents into u^k and x.
+__global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X, const float4* U,
+                                                 const float* gdelta, float4* gv, float4* gx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float invhi = 1.0f / xi.w;
+    const float3 ui = f3(U[i]);
+    const float di = gdelta[i];
+    const unsigned c = d.cnt[i];
+    const int nf = int(c & 0xffffu), nb = int(c >> 16);
+    float3 au = make_float3(0.f, 0.f, 0.f), xa = make_float3(0.f, 0.f, 0.f);
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
+        const float4 xj = X[j];
+        const float dj = gdelta[j];
+        const float3 uij = ui - f3(U[j]);
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD Ki = kern_d(r, invhi, p.cubic);
+        const KD Kj = xj.w == xi.w ? Ki : kern_d(r, 1.0f / xj.w, p.cubic);
+        au += (p.V * (di * Ki.G + dj * Kj.G)) * e;
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        const float eu = dot3(e, uij);
+        xa += (p.V * di) * (Ki.G * uij + (Ki.dG * ir * eu) * e);
+        xa += (p.V * dj) * (Kj.G * uij + (Kj.dG * ir * eu) * e);
+    }
+    for (int k = 0; k < nb; ++k) {
+        const unsigned b = d.nbr_b[size_t(k) * S + size_t(i)];
+        const float4 xb = d.bpos[b];
+        const float vb = d.bvol[b];
+        const float3 e = make_float3(xi.x - xb.x, xi.y - xb.y, xi.z - xb.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD K = kern_d(r, invhi, p.cubic);
+        au += (di * vb * K.G) * e;
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        xa += (di * vb) * (K.G * ui + (K.dG * ir * dot3(e, ui)) * e);
+    }
+    float4 v = gv[i];
+    v.x += au.x; v.y += au.y; v.z += au.z;
+    gv[i] = v;
+    float4 g = gx[i];
+    g.x += xa.x; g.y += xa.y; g.z += xa.z;
+    gx[i] = g;
+}
+
+// ------------------------------------------------------------------ Jacobi solve reverse
+// One transposed sweep: y = qbar / D, qbar' = qbar - (A_0 + f I)^T y, plus the sweep's share of
+// the cotangents of b, D and of each pair's coefficients (c, cv) and explicit x_ij.
+__global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float4* X, const unsigned char* rev,
+                                                     const float4* qk, const float4* qk1, const float4* qbar,
+                                                     float4* qbar_out, float4* bbar, float4* Dbar, float2* pc,
+                                                     float4* px) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float4 Di = d.jac_d[i];
+    const float4 qb = qbar[i];
+    const float3 y = make_float3(qb.x / Di.x, qb.y / Di.y, qb.z / Di.z);
+    const float3 qi = f3(qk[i]);
+    const int nf = int(d.cnt[i] & 0xffffu);
+    float3 aty = (1.0f + p.cg_factor) * y;
+    for (int k = 0; k < nf; ++k) {
+        const size_t at = size_t(k) * S + size_t(i);
+        const unsigned j = d.nbr_f[at];
+        const float2 cij = d.cg_coef[at];
+        const float2 cji = d.cg_coef[size_t(rev[at]) * S + j];
+        const float4 Dj = d.jac_d[j];
+        const float4 qbj = qbar[j];
+        const float3 yj = make_float3(qbj.x / Dj.x, qbj.y / Dj.y, qbj.z / Dj.z);
+        const float4 xj = X[j];
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        const float ye = dot3(y, e), yje = dot3(yj, e);
+        aty += p.dt * ((cij.x * y - (cij.y * ye) * e) - (cji.x * yj - (cji.y * yje) * e));
+        const float3 pp = qi - f3(qk[j]);
+        const float pe = dot3(pp, e);
+        float2 a = pc[at];
+        a.x += -p.dt * dot3(y, pp);
+        a.y += p.dt * pe * ye;
+        pc[at] = a;
+        float4 b = px[at];
+        const float3 t = (p.dt * cij.y) * (pe * y + ye * pp);
+        b.x += t.x; b.y += t.y; b.z += t.z;
+        px[at] = b;
+    }
+    qbar_out[i] = make_float4(qb.x - aty.x, qb.y - aty.y, qb.z - aty.z, 0.0f);
+    float4 bb = bbar[i];
+    bb.x += y.x; bb.y += y.y; bb.z += y.z;
+    bbar[i] = bb;
+    const float3 dq = f3(qk1[i]) - qi;
+    float4 db = Dbar[i];
+    db.x -= y.x * dq.x; db.y -= y.y * dq.y; db.z -= y.z * dq.z;
+    Dbar[i] = db;
+}
+
+// Inputs of one pair term of the solve set-up (k_cg_b), owner o, neighbour n.
+struct PairIn {
+    float3 e;          // x_o - x_n
+    float3 vo, vn;     // pre-solve velocities
+    float ro, rn;      // densities
+    float so, sn;      // surface-tension factors
+    float mo, mn;      // masses
+    float ho;          // support radius of the owner
+};
+struct PairBar {
+    float C, Cv;       // cotangents of c_on and cv_on
+    float3 Bb;         // cotangent of b_o (the pair's share of b is st_scale_o * (-c e))
+    float3 X;          // explicit cotangent of x_o - x_n
+};
+struct PairGrad {
+    float3 e, vo, vn;
+    float ro, rn, so, sn, sig, mu;
+};
+
+// Reverse of the pair term: c = mbar g_on, b share = -st_scale c e,
+// c_on = st_scale c + xsph/dt m_n/rho_n W, cv_on = 10 rho0 mu / rho_o mbar / rho_n G / ((d^2 + 0.01 h^2)(d + eps))
+// with g_on = (STW + dt (STG e.v_on - (s_o + s_n) invD STW / 2)) invD, invD = 2 / (rho_o + rho_n)
+// (MPSSPHNonPressureUtil.cuh:510-515,567-633; the forward is k_cg_b).
+__device__ PairGrad pair_reverse(const Params& p, const PairIn& in, const PairBar& bar) {
+    PairGrad g{};
+    const float r2 = dot3(in.e, in.e);
+    const float r = sqrtf(r2);
+    const float invh = 1.0f / in.ho;
+    const float invD = 2.0f / (in.ro + in.rn);
+    const KD st = kern_st(r, invh);
+    const KD kd = kern_d(r, invh, p.cubic);
+    const float3 vij = in.vo - in.vn;
+    const float ev = dot3(in.e, vij);
+    const float vdot = st.G * ev;
+    const float S = in.so + in.sn;
+    const float E = st.W + p.dt * (vdot - S * invD * 0.5f * st.W);
+    const float gg = E * invD;
+    const float mbar = 0.5f * (in.mo + in.mn);
+    const float c = mbar * gg;
+    const float st_scale = p.dt * p.sigma / in.mo;
+    const float xs = p.xsph * p.inv_dt;
+    const float den = r2 + 0.01f * in.ho * in.ho;
+    const float rr = r + kFltEps;
+    const float vs0 = 10.0f * p.rho0 / in.ro * mbar / in.rn;   // cv / (mu G / (den rr))
+    const float cv = p.visc * vs0 * kd.G / (den * rr);
+
+    float rbar = 0.0f;
+    float3 ebar = bar.X;
+    // cv
+    g.mu = bar.Cv * vs0 * kd.G / (den * rr);
+    g.ro = -bar.Cv * cv / in.ro;
+    g.rn = -bar.Cv * cv / in.rn;
+    rbar += bar.Cv * p.visc * vs0 * (kd.dG / (den * rr) - kd.G * 2.0f * r / (den * den * rr) - kd.G / (den * rr * rr));
+    // c_on
+    float cbar = bar.C * st_scale;
+    g.sig = bar.C * (p.dt / in.mo) * c;
+    g.rn += -bar.C * xs * in.mn * kd.W / (in.rn * in.rn);
+    rbar += bar.C * xs * (in.mn / in.rn) * kd.dW;
+    // b share: st_scale * (-c e)
+    const float3 Bt = st_scale * bar.Bb;
+    cbar += -dot3(Bt, in.e);
+    ebar -= c * Bt;
+    g.sig += -(p.dt / in.mo) * c * dot3(bar.Bb, in.e);
+    // c = mbar g; g = E invD
+    const float gbar = cbar * mbar;
+    const float Ebar = gbar * invD;
+    float invDbar = gbar * E;
+    const float stwbar = Ebar * (1.0f - 0.5f * p.dt * S * invD);
+    const float vdotbar = Ebar * p.dt;
+    const float Sbar = -Ebar * 0.5f * p.dt * invD * st.W;
+    invDbar += -Ebar * 0.5f * p.dt * S * st.W;
+    g.so = Sbar;
+    g.sn = Sbar;
+    const float rhob = -invDbar * invD * invD * 0.5f;
+    g.ro += rhob;
+    g.rn += rhob;
+    const float stgbar = vdotbar * ev;
+    const float evbar = vdotbar * st.G;
+    ebar += evbar * vij;
+    g.vo = evbar * in.e;
+    g.vn = (-evbar) * in.e;
+    rbar += stwbar * st.dW + stgbar * st.dG;
+    if (r > 0.0f) ebar += (rbar / r) * in.e;
+    g.e = ebar;
+    return g;
+}
+
+// The solve set-up's reverse: every pair term's cotangents (from the sweeps, the diagonal D and b)
+// into x, the pre-solve velocity, rho, the ST factor and the per-particle sigma / mu shares.
+__global__ void __launch_bounds__(kAB) k_adj_visc_coef(Dev d, Params p, const float4* X, const float4* V0,
+                                                        const unsigned char* rev, const float4* qbar0,
+                                                        const float4* bbar, const float4* Dbar, const float2* pc,
+                                                        const float4* px, float4* gv, float4* gx, float* grho,
+                                                        float* gsf, float* gsig, float* gmu) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float4 vi4 = V0[i];
+    const float2 ai = d.aux[i];
+    const float4 bbi = bbar[i];
+    const float4 Di = d.jac_d[i];
+    const int mi = int(Di.w);
+    const float4 Dbi4 = Dbar[i];
+    const float3 Dbi = make_float3(mi & 1 ? 0.f : Dbi4.x, mi & 2 ? 0.f : Dbi4.y, mi & 4 ? 0.f : Dbi4.z);
+    const int nf = int(d.cnt[i] & 0xffffu);
+    float3 gvi = f3(qbar0[i]) + (1.0f + p.cg_factor) * f3(bbi);
+    float3 gxi = make_float3(0.f, 0.f, 0.f);
+    float grhoi = 0.0f, gsfi = 0.0f, sig = 0.0f, mu = 0.0f;
+    const float dsumi = Dbi.x + Dbi.y + Dbi.z;
+    for (int k = 0; k < nf; ++k) {
+        const size_t at = size_t(k) * S + size_t(i);
+        const unsigned j = d.nbr_f[at];
+        const float4 xj = X[j];
+        const float4 vj4 = V0[j];
+        const float2 aj = d.aux[j];
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        const float3 e2 = mul3(e, e);
+        // term owned by i
+        {
+            const float2 cf = d.cg_coef[at];
+            const float2 a = pc[at];
+            const float4 xb = px[at];
+            PairIn in{e, f3(vi4), f3(vj4), ai.x, aj.x, ai.y, aj.y, vi4.w, vj4.w, xi.w};
+            PairBar bar;
+            bar.C = a.x + p.dt * dsumi;
+            bar.Cv = a.y - p.dt * dot3(Dbi, e2);
+            bar.Bb = f3(bbi);
+            bar.X = f3(xb) + (-2.0f * p.dt * cf.y) * mul3(e, Dbi);
+            const PairGrad g = pair_reverse(p, in, bar);
+            gxi += g.e;
+            gvi += g.vo;
+            grhoi += g.ro;
+            gsfi += g.so;
+            sig += g.sig;
+            mu += g.mu;
+        }
+        // term owned by j (i is its neighbour)
+        {
+            const size_t bt = size_t(rev[at]) * S + j;
+            const float2 cf = d.cg_coef[bt];
+            const float2 a = pc[bt];
+            const float4 xb = px[bt];
+            const float4 Dj = d.jac_d[j];
+            const int mj = int(Dj.w);
+            const float4 Dbj4 = Dbar[j];
+            const float3 Dbj = make_float3(mj & 1 ? 0.f : Dbj4.x, mj & 2 ? 0.f : Dbj4.y, mj & 4 ? 0.f : Dbj4.z);
+            const float3 ej = (-1.0f) * e;
+            PairIn in{ej, f3(vj4), f3(vi4), aj.x, ai.x, aj.y, ai.y, vj4.w, vi4.w, xj.w};
+            PairBar bar;
+            bar.C = a.x + p.dt * (Dbj.x + Dbj.y + Dbj.z);
+            bar.Cv = a.y - p.dt * dot3(Dbj, e2);
+            bar.Bb = f3(bbar[j]);
+            bar.X = f3(xb) + (-2.0f * p.dt * cf.y) * mul3(ej, Dbj);
+            const PairGrad g = pair_reverse(p, in, bar);
+            gxi -= g.e;
+            gvi += g.vn;
+            grhoi += g.rn;
+            gsfi += g.sn;
+        }
+    }
+    float4 v = gv[i];
+    v.x = gvi.x; v.y = gvi.y; v.z = gvi.z;
+    gv[i] = v;
+    float4 gg = gx[i];
+    gg.x += gxi.x; gg.y += gxi.y; gg.z += gxi.z;
+    gx[i] = gg;
+    grho[i] += grhoi;
+    gsf[i] = gsfi;
+    gsig[i] += sig;
+    gmu[i] += mu;
+}
+
+// Surface-tension factor reverse: s_i = sum_j m_j G_ij x_ij.(v_i - v_j) (k_st_factor).
+__global__ void __launch_bounds__(kAB) k_adj_stfac(Dev d, Params p, const float4* X, const float4* V0,
+                                                    const float* gsf, float4* gv, float4* gx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float invhi = 1.0f / xi.w;
+    const float4 vi = V0[i];
+    const float si = gsf[i];
+    const int nf = int(d.cnt[i] & 0xffffu);
+    float3 av = make_float3(0.f, 0.f, 0.f), xa = make_float3(0.f, 0.f, 0.f);
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
+        const float4 xj = X[j];
+        const float4 vj = V0[j];
+        const float sj = gsf[j];
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD Ki = kern_d(r, invhi, p.cubic);
+        const KD Kj = xj.w == xi.w ? Ki : kern_d(r, 1.0f / xj.w, p.cubic);
+        const float3 vij = f3(vi) - f3(vj);
+        const float wi = si * vj.w, wj = sj * vi.w;
+        av += (wi * Ki.G + wj * Kj.G) * e;
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        const float ev = dot3(e, vij);
+        xa += wi * (Ki.G * vij + (Ki.dG * ir * ev) * e);
+        xa += wj * (Kj.G * vij + (Kj.dG * ir * ev) * e);
+    }
+    float4 v = gv[i];
+    v.x += av.x; v.y += av.y; v.z += av.z;
+    gv[i] = v;
+    float4 g = gx[i];
+    g.x += xa.x; g.y += xa.y; g.z += xa.z;
+    gx[i] = g;
+}
+
+// ------------------------------------------------------------------ density + alpha reverse
+// gg_i = (gbar_i, sbar_i) from alphabar: alpha = 1 / f, f = s + |g|^2.
+__global__ void __launch_bounds__(kAB) k_adj_dens_a(Dev d, Params p, const float4* X, const float* galpha,
+                                                     float4* gg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float invhi = 1.0f / xi.w;
+    const unsigned c = d.cnt[i];
+    const int nf = int(c & 0xffffu), nb = int(c >> 16);
+    float3 gs = make_float3(0.f, 0.f, 0.f);
+    for (int k = 0; k < nf; ++k) {
+        const float4 xj = X[d.nbr_f[size_t(k) * S + size_t(i)]];
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        gs += (p.V * kern_d(sqrtf(dot3(e, e)), invhi, p.cubic).G) * e;
+    }
+    for (int k = 0; k < nb; ++k) {
+        const unsigned b = d.nbr_b[size_t(k) * S + size_t(i)];
+        const float4 xb = d.bpos[b];
+        const float3 e = make_float3(xi.x - xb.x, xi.y - xb.y, xi.z - xb.z);
+        gs += (d.bvol[b] * kern_d(sqrtf(dot3(e, e)), invhi, p.cubic).G) * e;
+    }
+    const float al = d.alpha[i];
+    const float fbar = al > 0.0f ? -al * al * galpha[i] : 0.0f;
+    gg[i] = make_float4(2.0f * fbar * gs.x, 2.0f * fbar * gs.y, 2.0f * fbar * gs.z, fbar);
+}
+
+__global__ void __launch_bounds__(kAB) k_adj_dens_b(Dev d, Params p, const float4* X, const float* grho,
+                                                     const float4* gg, float4* gx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const size_t S = size_t(p.slots);
+    const float4 xi = X[i];
+    const float invhi = 1.0f / xi.w;
+    const float rbi = grho[i] * p.rho0;
+    const float4 ggi = gg[i];
+    const float3 gbi = f3(ggi);
+    const unsigned c = d.cnt[i];
+    const int nf = int(c & 0xffffu), nb = int(c >> 16);
+    float3 xa = make_float3(0.f, 0.f, 0.f);
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
+        const float4 xj = X[j];
+        const float rbj = grho[j] * p.rho0;
+        const float4 ggj = gg[j];
+        const float3 gbj = f3(ggj);
+        const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD Ki = kern_d(r, invhi, p.cubic);
+        const KD Kj = xj.w == xi.w ? Ki : kern_d(r, 1.0f / xj.w, p.cubic);
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        // rho terms (radial), the s terms (|V G x|^2 = V^2 G^2 r^2, radial)
+        float rad = p.V * (rbi * Ki.dW + rbj * Kj.dW) * ir;
+        rad += p.V * p.V * 2.0f * (ggi.w * Ki.G * (r * Ki.dG + Ki.G) + ggj.w * Kj.G * (r * Kj.dG + Kj.G));
+        xa += rad * e;
+        // gradient-sum terms (vector)
+        xa += p.V * (Ki.G * gbi + (Ki.dG * ir * dot3(gbi, e)) * e);
+        xa -= p.V * (Kj.G * gbj + (Kj.dG * ir * dot3(gbj, e)) * e);
+    }
+    for (int k = 0; k < nb; ++k) {
+        const unsigned b = d.nbr_b[size_t(k) * S + size_t(i)];
+        const float4 xb = d.bpos[b];
+        const float vb = d.bvol[b];
+        const float3 e = make_float3(xi.x - xb.x, xi.y - xb.y, xi.z - xb.z);
+        const float r = sqrtf(dot3(e, e));
+        const KD K = kern_d(r, invhi, p.cubic);
+        const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+        xa += (vb * rbi * K.dW * ir) * e;
+        xa += vb * (K.G * gbi + (K.dG * ir * dot3(gbi, e)) * e);
+    }
+    float4 g = gx[i];
+    g.x += xa.x; g.y += xa.y; g.z += xa.z;
+    gx[i] = g;
+}
+
+// Per-scene sums of the sigma / mu shares (one block per scene, fixed order: deterministic).
+__global__ void k_adj_param_reduce(Dev d, Params p, const float* gsig, const float* gmu, double* gparam) {
+    __shared__ double sa[256], sb[256];
+    const int s = blockIdx.x;
+    const Scene& sc = d.scenes[s];
+    double a = 0.0, b = 0.0;
+    for (int i = sc.slot_begin + threadIdx.x; i < sc.slot_begin + sc.n; i += blockDim.x) {
+        a += double(gsig[i]);
+        b += double(gmu[i]);
+    }
+    sa[threadIdx.x] = a;
+    sb[threadIdx.x] = b;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) {
+            sa[threadIdx.x] += sa[threadIdx.x + w];
+            sb[threadIdx.x] += sb[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        gparam[2 * s] += sb[0];       // d/d viscosity
+        gparam[2 * s + 1] += sa[0];   // d/d surface tension
+    }
+}
+
+// ------------------------------------------------------------------ host side
+using host::fail;
+
+#define ADJ_TRY(expr)                                                                           \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(e_ == cudaErrorMemoryAllocation ? MPS_E_NOMEM : MPS_E_CUDA,             \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+struct Guard {
+    int prev = 0;
+    explicit Guard(int dev) { cudaGetDevice(&prev); cudaSetDevice(dev); }
+    ~Guard() { cudaSetDevice(prev); }
+};
+
+int nb_of(int n) { return (n + kAB - 1) / kAB; }
+
+size_t store_bytes(const mps_handle* h, int nsteps, int every) {
+    const size_t S = size_t(h->slots), cap = size_t(h->cfg.max_fluid_neighbors), K = size_t(h->cfg.fixed_iters);
+    const size_t ncp = size_t((nsteps + every - 1) / every);
+    const size_t state = S * (2 * sizeof(float4) + sizeof(unsigned));
+    size_t b = (ncp + 1 + size_t(every)) * state;
+    b += (3 * (K + 1) + 1) * S * sizeof(float4);            // tapes u (DF, CD), q, x
+    b += 2 * K * S * (sizeof(float) + 1) + S;               // stiffness, codes, collision codes
+    b += 9 * S * sizeof(float4) + 6 * S * sizeof(float);    // cotangents
+    b += cap * S * (sizeof(float2) + sizeof(float4) + 1);   // per-pair cotangents + reverse index
+    b += size_t(h->nscenes) * 2 * sizeof(double) + 64;
+    return b;
+}
+
+template <class T>
+cudaError_t alloc(T** p, size_t count, size_t& total) {
+    total += count * sizeof(T);
+    return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+}
+
+int ensure_store(mps_handle* h, int nsteps, int every) {
+    if (!h->adj) h->adj = new AdjointStore();
+    AdjointStore& A = *h->adj;
+    const int K = h->cfg.fixed_iters;
+    const int ncp = (nsteps + every - 1) / every;
+    if (A.slots == h->slots && A.K == K && A.ncp_cap >= ncp && A.every_cap >= every &&
+        A.cap == h->cfg.max_fluid_neighbors && A.nscenes == h->nscenes && A.cp_pos)
+        return MPS_OK;
+    A.free_all();
+    A.slots = h->slots;
+    A.K = K;
+    A.ncp_cap = ncp;
+    A.every_cap = every;
+    A.cap = h->cfg.max_fluid_neighbors;
+    A.nscenes = h->nscenes;
+    A.n = h->n;
+    const size_t S = size_t(h->slots), cap = size_t(A.cap);
+    size_t& t = A.bytes;
+    ADJ_TRY(alloc(&A.cp_pos, S * ncp, t));
+    ADJ_TRY(alloc(&A.cp_vel, S * ncp, t));
+    ADJ_TRY(alloc(&A.cp_ids, S * ncp, t));
+    ADJ_TRY(alloc(&A.fin_pos, S, t));
+    ADJ_TRY(alloc(&A.fin_vel, S, t));
+    ADJ_TRY(alloc(&A.fin_ids, S, t));
+    ADJ_TRY(alloc(&A.seg_pos, S * every, t));
+    ADJ_TRY(alloc(&A.seg_vel, S * every, t));
+    ADJ_TRY(alloc(&A.seg_ids, S * every, t));
+    ADJ_TRY(alloc(&A.t_udf, S * (K + 1), t));
+    ADJ_TRY(alloc(&A.t_ucd, S * (K + 1), t));
+    ADJ_TRY(alloc(&A.t_q, S * (K + 1), t));
+    ADJ_TRY(alloc(&A.t_x, S, t));
+    ADJ_TRY(alloc(&A.t_kdf, S * K, t));
+    ADJ_TRY(alloc(&A.t_kcd, S * K, t));
+    ADJ_TRY(alloc(&A.t_cdf, S * K, t));
+    ADJ_TRY(alloc(&A.t_ccd, S * K, t));
+    ADJ_TRY(alloc(&A.t_adv, S, t));
+    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.gg};
+    for (float4** q : f4) ADJ_TRY(alloc(q, S, t));
+    ADJ_TRY(alloc(&A.gx_id, size_t(std::max<int64_t>(h->n, 1)), t));
+    ADJ_TRY(alloc(&A.gv_id, size_t(std::max<int64_t>(h->n, 1)), t));
+    float** f1[] = {&A.grho, &A.galpha, &A.gdelta, &A.gsf, &A.gsig, &A.gmu};
+    for (float** q : f1) ADJ_TRY(alloc(q, S, t));
+    ADJ_TRY(alloc(&A.pc, S * cap, t));
+    ADJ_TRY(alloc(&A.px, S * cap, t));
+    ADJ_TRY(alloc(&A.rev, S * cap, t));
+    ADJ_TRY(alloc(&A.gparam, 2 * size_t(h->nscenes), t));
+    ADJ_TRY(alloc(&A.flag, 1, t));
+    ADJ_TRY(alloc(&A.ctr_save, 1, t));
+    A.cp_cur.assign(size_t(ncp), 0);
+    A.seg_cur.assign(size_t(every), 0);
+    // zero what the kernels read before writing (padding slots of the cotangents)
+    for (float4** q : f4) ADJ_TRY(cudaMemset(*q, 0, S * sizeof(float4)));
+    for (float** q : f1) ADJ_TRY(cudaMemset(*q, 0, S * sizeof(float)));
+    return MPS_OK;
+}
+
+cudaError_t copy_state(mps_handle* h, int buf, float4* pos, float4* vel, unsigned* ids, bool save, cudaStream_t s) {
+    const size_t S = size_t(h->slots);
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    cudaError_t e;
+    if (save) {
+        if ((e = cudaMemcpyAsync(pos, h->pos[buf], S * sizeof(float4), k, s))) return e;
+        if ((e = cudaMemcpyAsync(vel, h->vel[buf], S * sizeof(float4), k, s))) return e;
+        return cudaMemcpyAsync(ids, h->ids[buf], S * sizeof(unsigned), k, s);
+    }
+    if ((e = cudaMemcpyAsync(h->pos[buf], pos, S * sizeof(float4), k, s))) return e;
+    if ((e = cudaMemcpyAsync(h->vel[buf], vel, S * sizeof(float4), k, s))) return e;
+    return cudaMemcpyAsync(h->ids[buf], ids, S * sizeof(unsigned), k, s);
+}
+
+// One pressure solve recorded: u^k before each iteration, kappa^k and the branch codes.
+int taped_pressure(mps_handle* h, int mode, float4* tu, float* tk, unsigned char* tc, cudaStream_t s) {
+    const Params p = host::make_params(h);
+    Dev d = host::make_dev(h, h->cur);
+    const int bs = host::block_size(h);
+    const size_t S = size_t(h->slots);
+    const int K = h->cfg.fixed_iters;
+    launch_solver_init(d, p, s);
+    for (int k = 0; k < K; ++k) {
+        ADJ_TRY(cudaMemcpyAsync(tu + size_t(k) * S, h->vel[h->cur], S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+        d.tape_code = tc + size_t(k) * S;
+        launch_pressure_A(d, p, mode, bs, 0ull, 0, s);
+        ADJ_TRY(cudaMemcpyAsync(tk + size_t(k) * S, h->kappa, S * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        d.tape_code = nullptr;
+        launch_pressure_B(d, p, bs, 0ull, 0, 0, s);
+    }
+    ADJ_TRY(cudaMemcpyAsync(tu + size_t(K) * S, h->vel[h->cur], S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    launch_solver_finish(d, p, mode == 0 ? 0 : 2, s);
+    ADJ_TRY(cudaGetLastError());
+    return MPS_OK;
+}
+
+// The step of mps_step, run phase by phase with recording (bit-identical to the plain step).
+int taped_step(mps_handle* h, cudaStream_t s) {
+    AdjointStore& A = *h->adj;
+    int r;
+    if ((r = host::run_phase(h, MPS_PHASE_SORT, s))) return r;
+    if ((r = host::run_phase(h, MPS_PHASE_NEIGHBORS, s))) return r;
+    if ((r = host::run_phase(h, MPS_PHASE_BVOLUME, s))) return r;
+    if ((r = host::run_phase(h, MPS_PHASE_DENSITY_ALPHA, s))) return r;
+    if ((r = taped_pressure(h, 0, A.t_udf, A.t_kdf, A.t_cdf, s))) return r;
+    {
+        const Params p = host::make_params(h);
+        const Dev d = host::make_dev(h, h->cur);
+        const int bs = host::block_size(h);
+        const size_t S = size_t(h->slots);
+        launch_st_factor(d, p, bs, s);
+        launch_cg_b(d, p, bs, s);
+        ADJ_TRY(cudaMemcpyAsync(A.t_q, h->cg_x, S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+        launch_solver_init(d, p, s);
+        for (int k = 0; k < A.K; ++k)
+            launch_jacobi(d, p, bs, 0ull, 0, 0, A.t_q + size_t(k) * S, A.t_q + size_t(k + 1) * S, s);
+        launch_solver_finish(d, p, 1, s);
+        launch_jacobi_finish(d, p, A.t_q + size_t(A.K) * S, s);
+        ADJ_TRY(cudaGetLastError());
+    }
+    if ((r = taped_pressure(h, 1, A.t_ucd, A.t_kcd, A.t_ccd, s))) return r;
+    {
+        const Params p = host::make_params(h);
+        Dev d = host::make_dev(h, h->cur);
+        ADJ_TRY(cudaMemcpyAsync(A.t_x, h->pos[h->cur], size_t(h->slots) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+        d.tape_adv = A.t_adv;
+        launch_advect(d, p, s);
+        ADJ_TRY(cudaGetLastError());
+    }
+    return MPS_OK;
+}
+
+// Reverse of the step just recorded: cotangents of its output (ID order, A.gx_id / A.gv_id) are
+// replaced by those of its input.
+int adjoint_step(mps_handle* h, cudaStream_t s) {
+    AdjointStore& A = *h->adj;
+    const Params p = host::make_params(h);
+    const Dev d = host::make_dev(h, h->cur);
+    const size_t S = size_t(h->slots), cap = size_t(A.cap);
+    const int K = A.K;
+    const int nb = nb_of(h->slots);
+    k_adj_gather<<<nb, kAB, 0, s>>>(d, p, A.gx_id, A.gv_id, A.gx, A.gv, A.grho, A.galpha);
+    k_adj_rev<<<nb, kAB, 0, s>>>(d, p, A.rev, A.flag);
+    k_adj_advect<<<nb, kAB, 0, s>>>(d, p, A.t_adv, A.gx, A.gv);
+    // constant-density solve
+    for (int k = K - 1; k >= 0; --k) {
+        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_kcd + size_t(k) * S, A.t_ccd + size_t(k) * S, A.gv, A.gdelta,
+                                     A.grho, A.galpha, A.gx);
+        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_ucd + size_t(k) * S, A.gdelta, A.gv, A.gx);
+    }
+    // viscosity + surface tension (Jacobi)
+    ADJ_TRY(cudaMemsetAsync(A.pc, 0, cap * S * sizeof(float2), s));
+    ADJ_TRY(cudaMemsetAsync(A.px, 0, cap * S * sizeof(float4), s));
+    ADJ_TRY(cudaMemsetAsync(A.bbar, 0, S * sizeof(float4), s));
+    ADJ_TRY(cudaMemsetAsync(A.Dbar, 0, S * sizeof(float4), s));
+    ADJ_TRY(cudaMemcpyAsync(A.qbar0, A.gv, S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    float4* qa = A.qbar0;
+    float4* qb = A.qbar1;
+    for (int k = K - 1; k >= 0; --k) {
+        k_adj_jacobi<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.rev, A.t_q + size_t(k) * S, A.t_q + size_t(k + 1) * S, qa, qb,
+                                         A.bbar, A.Dbar, A.pc, A.px);
+        std::swap(qa, qb);
+    }
+    const float4* V0 = A.t_udf + size_t(K) * S;   // pre-solve velocity = DF output
+    k_adj_visc_coef<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.rev, qa, A.bbar, A.Dbar, A.pc, A.px, A.gv, A.gx, A.grho,
+                                        A.gsf, A.gsig, A.gmu);
+    k_adj_stfac<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.gsf, A.gv, A.gx);
+    // divergence-free solve
+    for (int k = K - 1; k >= 0; --k) {
+        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_kdf + size_t(k) * S, A.t_cdf + size_t(k) * S, A.gv, A.gdelta,
+                                     A.grho, A.galpha, A.gx);
+        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_udf + size_t(k) * S, A.gdelta, A.gv, A.gx);
+    }
+    // gravity is the identity; density and alpha
+    k_adj_dens_a<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.galpha, A.gg);
+    k_adj_dens_b<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.grho, A.gg, A.gx);
+    k_adj_scatter<<<nb, kAB, 0, s>>>(d, p, A.gx, A.gv, A.gx_id, A.gv_id);
+    ADJ_TRY(cudaGetLastError());
+    return MPS_OK;
+}
+
+int check_adjoint_config(mps_handle* h) {
+    if (h->cfg.fixed_iters <= 0) return fail(MPS_E_INVALID, "adjoint needs fixed_iters > 0");
+    if (h->cfg.visc_solver != MPS_VISC_JACOBI) return fail(MPS_E_INVALID, "adjoint needs visc_solver = MPS_VISC_JACOBI");
+    if (h->cfg.volume_accumulate) return fail(MPS_E_INVALID, "adjoint needs volume_accumulate = 0");
+    if (h->cfg.max_fluid_neighbors > 255) return fail(MPS_E_INVALID, "adjoint needs max_fluid_neighbors <= 255");
+    return MPS_OK;
+}
+
+}  // namespace
+
+namespace host {
+void adjoint_release(mps_handle* h) {
+    if (!h->adj) return;
+    h->adj->free_all();
+    delete h->adj;
+    h->adj = nullptr;
+}
+}  // namespace host
+
+}  // namespace mpsg
+
+using namespace mpsg;
+
+extern "C" {
+
+int64_t mps_adjoint_memory(mps_handle* h, int32_t nsteps, int32_t every) {
+    if (!h || !h->layout_ready || nsteps <= 0 || every <= 0) return -1;
+    return int64_t(store_bytes(h, nsteps, every));
+}
+
+int mps_adjoint_forward(mps_handle* h, int32_t nsteps, int32_t every, void* stream) {
+    int r = host::check_ready(h);
+    if (r) return r;
+    if ((r = check_adjoint_config(h))) return r;
+    if (nsteps <= 0 || every <= 0) return fail(MPS_E_INVALID, "nsteps and checkpoint_every must be positive");
+    Guard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((r = ensure_store(h, nsteps, every))) return r;
+    AdjointStore& A = *h->adj;
+    A.nsteps = nsteps;
+    A.every = every;
+    A.ready = false;
+    const size_t S = size_t(h->slots);
+    for (int t = 0; t < nsteps; ++t) {
+        if (t % every == 0) {
+            const int c = t / every;
+            ADJ_TRY(copy_state(h, h->cur, A.cp_pos + size_t(c) * S, A.cp_vel + size_t(c) * S, A.cp_ids + size_t(c) * S,
+                               true, s));
+            A.cp_cur[size_t(c)] = h->cur;
+        }
+        if ((r = host::step_n(h, 1, s))) return r;
+    }
+    ADJ_TRY(copy_state(h, h->cur, A.fin_pos, A.fin_vel, A.fin_ids, true, s));
+    A.fin_cur = h->cur;
+    A.fin_steps = h->steps;
+    A.ready = true;
+    return MPS_OK;
+}
+
+int mps_adjoint_backward(mps_handle* h, const float* g_pos4, const float* g_vel4, float* g_pos0, float* g_vel0,
+                         double* g_param2, void* stream) {
+    int r = host::check_ready(h);
+    if (r) return r;
+    if ((r = check_adjoint_config(h))) return r;
+    if (!h->adj || !h->adj->ready) return fail(MPS_E_STATE, "mps_adjoint_forward first");
+    Guard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    AdjointStore& A = *h->adj;
+    const size_t S = size_t(h->slots), N = size_t(h->n);
+    ADJ_TRY(cudaMemcpyAsync(A.ctr_save, h->ctr, sizeof(StepCounters), cudaMemcpyDeviceToDevice, s));
+    if (g_pos4) ADJ_TRY(cudaMemcpyAsync(A.gx_id, g_pos4, N * sizeof(float4), cudaMemcpyHostToDevice, s));
+    else ADJ_TRY(cudaMemsetAsync(A.gx_id, 0, N * sizeof(float4), s));
+    if (g_vel4) ADJ_TRY(cudaMemcpyAsync(A.gv_id, g_vel4, N * sizeof(float4), cudaMemcpyHostToDevice, s));
+    else ADJ_TRY(cudaMemsetAsync(A.gv_id, 0, N * sizeof(float4), s));
+    ADJ_TRY(cudaMemsetAsync(A.gparam, 0, 2 * size_t(h->nscenes) * sizeof(double), s));
+    ADJ_TRY(cudaMemsetAsync(A.flag, 0, sizeof(int), s));
+    const int nseg = (A.nsteps + A.every - 1) / A.every;
+    const Params p = host::make_params(h);
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int t0 = seg * A.every, t1 = std::min(A.nsteps, t0 + A.every);
+        // start states of the segment's steps, recomputed from the checkpoint with the plain step
+        h->cur = A.cp_cur[size_t(seg)];
+        ADJ_TRY(copy_state(h, h->cur, A.cp_pos + size_t(seg) * S, A.cp_vel + size_t(seg) * S, A.cp_ids + size_t(seg) * S,
+                           false, s));
+        for (int t = t0; t < t1; ++t) {
+            const int k = t - t0;
+            ADJ_TRY(copy_state(h, h->cur, A.seg_pos + size_t(k) * S, A.seg_vel + size_t(k) * S, A.seg_ids + size_t(k) * S,
+                               true, s));
+            A.seg_cur[size_t(k)] = h->cur;
+            if (t + 1 < t1 && (r = host::step_n(h, 1, s))) return r;
+        }
+        for (int t = t1 - 1; t >= t0; --t) {
+            const int k = t - t0;
+            h->cur = A.seg_cur[size_t(k)];
+            ADJ_TRY(copy_state(h, h->cur, A.seg_pos + size_t(k) * S, A.seg_vel + size_t(k) * S, A.seg_ids + size_t(k) * S,
+                               false, s));
+            if ((r = taped_step(h, s))) return r;
+            if ((r = adjoint_step(h, s))) return r;
+            const Dev d = host::make_dev(h, h->cur);
+            k_adj_param_reduce<<<h->nscenes, 256, 0, s>>>(d, p, A.gsig, A.gmu, A.gparam);
+            ADJ_TRY(cudaMemsetAsync(A.gsig, 0, S * sizeof(float), s));
+            ADJ_TRY(cudaMemsetAsync(A.gmu, 0, S * sizeof(float), s));
+            ADJ_TRY(cudaGetLastError());
+        }
+    }
+    int flag = 0, ctr_flags = 0;
+    ADJ_TRY(cudaMemcpyAsync(&flag, A.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ADJ_TRY(cudaMemcpyAsync(&ctr_flags, &h->ctr->flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ADJ_TRY(cudaStreamSynchronize(s));
+    if (g_pos0) ADJ_TRY(cudaMemcpy(g_pos0, A.gx_id, N * sizeof(float4), cudaMemcpyDeviceToHost));
+    if (g_vel0) ADJ_TRY(cudaMemcpy(g_vel0, A.gv_id, N * sizeof(float4), cudaMemcpyDeviceToHost));
+    if (g_param2) ADJ_TRY(cudaMemcpy(g_param2, A.gparam, 2 * size_t(h->nscenes) * sizeof(double), cudaMemcpyDeviceToHost));
+    // leave the handle at the final state with its counters as they were
+    h->cur = A.fin_cur;
+    ADJ_TRY(copy_state(h, h->cur, A.fin_pos, A.fin_vel, A.fin_ids, false, s));
+    ADJ_TRY(cudaMemcpyAsync(h->ctr, A.ctr_save, sizeof(StepCounters), cudaMemcpyDeviceToDevice, s));
+    h->steps = A.fin_steps;
+    ADJ_TRY(cudaStreamSynchronize(s));
+    if (ctr_flags & 1) return fail(MPS_E_OVERFLOW, "neighbour list capacity exceeded during the adjoint");
+    if (flag & 1) return fail(MPS_E_STATE, "asymmetric neighbour lists: the gather-form adjoint needs symmetric lists");
+    return MPS_OK;
+}
+
+}  // extern "C"

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "mps_c.h"
+#include "handle.cuh"
 #include "mps_internal.cuh"
 
 using namespace mpsg;
@@ -61,72 +62,6 @@ inline int host_cell(float x, float o, float inv, int dim) {
 
 }  // namespace
 
-struct mps_handle {
-    int device = 0;
-    mps_material mat{};
-    mps_physics phys{};
-    mps_config cfg{};
-    bool batched = false;
-    int nscenes = 1;
-    std::vector<double> boxes;           // 6 per scene (batched); single scene uses phys
-    std::vector<int64_t> fluid_off, bnd_off;
-    std::vector<Scene> scenes;
-    int64_t n = 0, nb = 0;
-    int slots = 0;
-    unsigned long long total_cells = 0;
-    int key_bits = 0;
-    bool have_fluid = false;
-    bool have_boundary = false;
-    bool bvol_given = false;
-    bool layout_ready = false;
-    int cur = 0;                         // state buffer holding the current order
-    int64_t steps = 0;
-
-    // device memory
-    float4* pos[2] = {nullptr, nullptr};
-    float4* vel[2] = {nullptr, nullptr};
-    unsigned* ids[2] = {nullptr, nullptr};
-    unsigned long long* slot_key = nullptr;
-    uint2* ftable = nullptr;
-    uint2* btable = nullptr;
-    Scene* d_scenes = nullptr;
-    int* chunk_scene = nullptr;
-    unsigned* nbr_f = nullptr;
-    unsigned* nbr_b = nullptr;
-    unsigned* cnt = nullptr;
-    unsigned short* nbr_l = nullptr;
-    Stage* stage = nullptr;
-    float *rho = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
-    float2* aux = nullptr;
-    float4* color = nullptr;
-    float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr;
-    float2* cg_coef = nullptr;
-    float4* bpos = nullptr;
-    float* bvol = nullptr;
-    double* partial = nullptr;
-    SceneSolve* solve = nullptr;
-    StepCounters* ctr = nullptr;
-    int* scene_iters = nullptr;
-    double* scene_err = nullptr;
-    unsigned long long *keys = nullptr, *keys_tmp = nullptr;
-    unsigned *vals = nullptr, *vals_tmp = nullptr;
-    unsigned* sort_counts = nullptr;
-    float4 *stage_pos = nullptr, *stage_vel = nullptr;   // ID-order staging for I/O
-    int* h_nactive = nullptr;                            // pinned
-
-    std::vector<uint32_t> bperm;        // sorted boundary index -> user boundary index
-    std::vector<float4> bpos_user;      // boundary positions as given (x,y,z,h) in user order
-    std::vector<float> bvol_user;
-
-    cudaStream_t cap_stream = nullptr;
-    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (cur, nsteps) -> exec
-    std::vector<cudaGraph_t> graph_defs;
-
-    ~mps_handle() { release(); if (cap_stream) { cudaStreamDestroy(cap_stream); cap_stream = nullptr; } }
-    void drop_graphs();
-    void release();   // frees every device buffer and forgets the layout
-};
-
 void mps_handle::drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
@@ -139,6 +74,7 @@ void mps_handle::release() {
     cudaGetDevice(&prev);
     cudaSetDevice(device);
     drop_graphs();
+    mpsg::host::adjoint_release(this);
     void** ptrs[] = {(void**)&pos[0], (void**)&pos[1], (void**)&vel[0], (void**)&vel[1], (void**)&ids[0],
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
                      (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&nbr_l, (void**)&stage, (void**)&rho,
@@ -195,6 +131,7 @@ Params make_params(const mps_handle* h) {
     p.min_iter_cd = c.cd_min_iter;
     p.max_iter = c.max_iter;
     p.cg_max_iter = c.cg_max_iter;
+    p.visc_solver = c.visc_solver == MPS_VISC_JACOBI ? 1 : 0;
     p.df_tol = float(c.df_tol);
     p.cd_tol = float(c.cd_tol);
     p.cg_tol = float(c.cg_tol);
@@ -236,6 +173,9 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.cg_ap = h->cg_ap;
     d.cg_b = h->cg_b;
     d.cg_coef = h->cg_coef;
+    d.jac_d = h->cg_ap;
+    d.tape_code = nullptr;
+    d.tape_adv = nullptr;
     d.bpos = h->bpos;
     d.bvol = h->bvol;
     d.partial = h->partial;
@@ -448,7 +388,9 @@ int eager_loop(mps_handle* h, cudaStream_t s, int kind /*0 DF,1 CG,2 CD*/) {
     const int bs = block_size(h);
     const int cap = (h->cfg.fixed_iters > 0 ? h->cfg.fixed_iters : (kind == 1 ? h->cfg.cg_max_iter : h->cfg.max_iter)) + 2;
     for (int it = 0; it < cap; ++it) {
-        if (kind == 1) {
+        if (kind == 1 && p.visc_solver == 1) {
+            launch_jacobi(d, p, bs, 0ull, 0, 0, nullptr, nullptr, s);
+        } else if (kind == 1) {
             launch_cg_ap(d, p, bs, 0ull, 0, s);
             launch_cg_update(d, p, bs, s);
             launch_cg_dir(d, p, bs, 0ull, 0, 0, s);
@@ -486,12 +428,13 @@ int run_phase(mps_handle* h, int phase, cudaStream_t s) {
             const Dev d = make_dev(h, h->cur);
             launch_st_factor(d, p, bs, s);
             launch_cg_b(d, p, bs, s);
-            launch_cg_ax0(d, p, bs, s);
+            if (!p.visc_solver) launch_cg_ax0(d, p, bs, s);
             launch_solver_init(d, p, s);
             const int r = eager_loop(h, s, 1);
             if (r) return r;
             launch_solver_finish(d, p, 1, s);
-            launch_cg_finish(d, p, s);
+            if (p.visc_solver) launch_jacobi_finish(d, p, nullptr, s);
+            else launch_cg_finish(d, p, s);
             break;
         }
         case MPS_PHASE_ADVECT: launch_advect(make_dev(h, h->cur), p, s); break;
@@ -604,7 +547,7 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         launch_solver_finish(d, p, 0, c.s);
         launch_st_factor(d, p, bs, c.s);
         launch_cg_b(d, p, bs, c.s);
-        launch_cg_ax0(d, p, bs, c.s);
+        if (!p.visc_solver) launch_cg_ax0(d, p, bs, c.s);
         launch_solver_init(d, p, c.s);
         launch_set_cond(d, hcg, c.s);
         MPS_CAP_TRY(cudaGetLastError());
@@ -613,16 +556,21 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         {
             Capture b{body, h->cap_stream, {}};
             MPS_CAP_TRY(seg_begin(b));
-            launch_cg_ap(d, p, bs, hcg, 1, b.s);
-            launch_cg_update(d, p, bs, b.s);
-            launch_cg_dir(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+            if (p.visc_solver) {
+                launch_jacobi(d, p, bs, hcg, 1, loop_limit(h, 1), nullptr, nullptr, b.s);
+            } else {
+                launch_cg_ap(d, p, bs, hcg, 1, b.s);
+                launch_cg_update(d, p, bs, b.s);
+                launch_cg_dir(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+            }
             MPS_CAP_TRY(cudaGetLastError());
             MPS_CAP_TRY(seg_end(b));
         }
         // constant density
         MPS_CAP_TRY(seg_begin(c));
         launch_solver_finish(d, p, 1, c.s);
-        launch_cg_finish(d, p, c.s);
+        if (p.visc_solver) launch_jacobi_finish(d, p, nullptr, c.s);
+        else launch_cg_finish(d, p, c.s);
         launch_solver_init(d, p, c.s);
         launch_set_cond(d, hcd, c.s);
         MPS_CAP_TRY(cudaGetLastError());
@@ -713,7 +661,41 @@ bool field_info(mps_handle* h, const std::string& n, FieldInfo& f) {
     return true;
 }
 
+// mps_step's work once the arguments are checked: graph per step, or eager phases.
+int step_n_impl(mps_handle* h, int nsteps, cudaStream_t s) {
+    if (!h->cfg.use_graph) {
+        for (int k = 0; k < nsteps; ++k) {
+            const int e = step_eager(h, s);
+            if (e) return e;
+            h->steps++;
+        }
+        return MPS_OK;
+    }
+    // one graph per step; graphs for both buffer parities are cached
+    for (int k = 0; k < nsteps; ++k) {
+        cudaGraphExec_t ex;
+        const int e = get_graph(h, 1, &ex);
+        if (e) return e;
+        MPS_CUDA_TRY(cudaGraphLaunch(ex, s));
+        h->cur = 1 - h->cur;
+        h->steps++;
+    }
+    return MPS_OK;
+}
+
 }  // namespace
+
+namespace mpsg {
+namespace host {
+int fail(int code, const std::string& msg) { return ::fail(code, msg); }
+Params make_params(const mps_handle* h) { return ::make_params(h); }
+Dev make_dev(const mps_handle* h, int sorted_buf) { return ::make_dev(h, sorted_buf); }
+int block_size(const mps_handle* h) { return ::block_size(h); }
+int run_phase(mps_handle* h, int phase, cudaStream_t s) { return ::run_phase(h, phase, s); }
+int step_n(mps_handle* h, int nsteps, cudaStream_t s) { return step_n_impl(h, nsteps, s); }
+int check_ready(mps_handle* h) { return ::check_ready(h); }
+}  // namespace host
+}  // namespace mpsg
 
 // ===================================================================== C ABI
 extern "C" {
@@ -740,6 +722,7 @@ void mps_default_config(mps_config* c) {
     c->block_size = 128;
     c->stage = 0;
     c->sort_digit_bits = 8;
+    c->visc_solver = MPS_VISC_CG;
 }
 
 // SPHMaterial() + SetRadius(h): V = h^3 / 48 * 3.141592, mass = density * V
@@ -775,6 +758,7 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (h->cfg.max_iter <= 0) h->cfg.max_iter = 100;
     if (h->cfg.cg_max_iter <= 0) h->cfg.cg_max_iter = 100;
     if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;
+    if (h->cfg.visc_solver != MPS_VISC_JACOBI) h->cfg.visc_solver = MPS_VISC_CG;
     *out = h;
     return MPS_OK;
 }
@@ -950,25 +934,7 @@ int mps_step(mps_handle* h, int32_t nsteps, void* stream) {
     if (r) return r;
     if (nsteps < 0) return fail(MPS_E_INVALID, "nsteps < 0");
     DeviceGuard g(h->device);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (!h->cfg.use_graph) {
-        for (int k = 0; k < nsteps; ++k) {
-            const int e = step_eager(h, s);
-            if (e) return e;
-            h->steps++;
-        }
-        return MPS_OK;
-    }
-    // one graph per step; graphs for both buffer parities are cached
-    for (int k = 0; k < nsteps; ++k) {
-        cudaGraphExec_t ex;
-        const int e = get_graph(h, 1, &ex);
-        if (e) return e;
-        MPS_CUDA_TRY(cudaGraphLaunch(ex, s));
-        h->cur = 1 - h->cur;
-        h->steps++;
-    }
-    return MPS_OK;
+    return step_n_impl(h, nsteps, static_cast<cudaStream_t>(stream));
 }
 
 int mps_step_host(mps_handle* h, float* pos4, float* vel4, int32_t nsteps, void* stream) {

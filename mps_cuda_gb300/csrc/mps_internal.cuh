@@ -18,6 +18,7 @@ namespace mpsg {
 constexpr int kPad = 256;          // slot padding unit per scene
 constexpr int kChunk = 64;         // granularity of the slot -> scene table
 constexpr float kHRatio = 4.0f;    // support radius = 4 x particle radius
+constexpr float kFltEps = 1.1920928955078125e-07f;   // FLT_EPSILON (viscosity denominator)
 
 // Per-scene constants.
 struct Scene {
@@ -77,6 +78,7 @@ struct Params {
     int nscenes;
     int fixed_iters;
     int min_iter_df, min_iter_cd, max_iter, cg_max_iter;
+    int visc_solver;              // 0 CG, 1 Jacobi
     float df_tol, cd_tol, cg_tol; // stored as float for the kernel args; compared in FP64
     double df_tol_d, cd_tol_d, cg_tol_d;
 };
@@ -106,6 +108,9 @@ struct Dev {
     float4* color;
     float4 *cg_x, *cg_r, *cg_p, *cg_ap, *cg_b;
     float2* cg_coef;              // per fluid pair, interleaved like nbr_f: (c_ij, cv_ij) of the CG operator
+    float4* jac_d;                // Jacobi: diagonal of A_0 + f I per component (aliases cg_ap)
+    unsigned char* tape_code;     // adjoint recording (null in plain steps): stiffness branch per slot
+    unsigned char* tape_adv;      // adjoint recording: collision branch per slot (2 bits per axis)
     const float4* bpos;           // boundary (x, y, z, h)
     float* bvol;
     double* partial;              // per-block FP64 partial sums (2 per block)
@@ -234,6 +239,11 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, cudaStream_t s);
 void launch_cg_dir(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    cudaStream_t s);
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);
+// Jacobi sweep of the viscosity/surface-tension system; src/dst null = the two iterate buffers
+// chosen by the scene's loop counter (graph form), else explicit (adjoint recording).
+void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                   const float4* src, float4* dst, cudaStream_t s);
+void launch_jacobi_finish(const Dev& d, const Params& p, const float4* src, cudaStream_t s);
 void launch_advect(const Dev& d, const Params& p, cudaStream_t s);
 void launch_stats(const Dev& d, const Params& p, cudaStream_t s);
 

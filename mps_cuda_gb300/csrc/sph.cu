@@ -22,7 +22,6 @@ namespace mpsg {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr float kFltEps = 1.1920928955078125e-07f;
 
 __device__ __forceinline__ int block_scene(const Dev& d, int bs) {
     return d.chunk_scene[(blockIdx.x * bs) / kChunk];
@@ -488,15 +487,20 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         }
         const float delta = p.V * df + db;
         const float r = d.rho[i] * p.inv_rho0;
-        float kap = mode == 0 ? fminf(delta * p.dt, r + p.dt * delta - 0.8f) : r + p.dt * delta - 1.0f;
+        const float ka = delta * p.dt;
+        const float kb = r + p.dt * delta - 0.8f;
+        float kap = mode == 0 ? fminf(ka, kb) : r + p.dt * delta - 1.0f;
+        unsigned char code = 0;   // 0 clamped, 1 the dt*delta branch of DF, 2 the density branch
         if (kap > 0.0f) {
             err = kap;
+            code = (mode == 0 && ka <= kb) ? 1 : 2;
             kap *= d.alpha[i] * (p.inv_dt * p.inv_dt);
         } else {
             kap = 0.0f;
         }
         d.kappa[i] = kap;
         d.delta[i] = delta;
+        if (d.tape_code) d.tape_code[i] = code;
     }
     const double2 bs2 = block_sum2_f<BS>(err, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
@@ -669,6 +673,7 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     const float vs = 10.0f * p.rho0 * p.visc / ai.x;
     const int nf = int(d.cnt[i] & 0xffffu);
     float bx = 0.0f, by = 0.0f, bz = 0.0f;
+    float csum = 0.0f, vx2 = 0.0f, vy2 = 0.0f, vz2 = 0.0f;   // Jacobi diagonal sums
     for (int k = 0; k < nf; ++k) {
         const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
         const float4 xj = d.pos[j];
@@ -693,9 +698,22 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
         cf.x = st_scale * c + xs_scale * (vj.w * inv_rj) * w;
         cf.y = vs * mbar * inv_rj / (d2 + eps_h2) * G / (dist + kFltEps);
         d.cg_coef[size_t(k) * stride + size_t(i)] = cf;
+        csum += cf.x;
+        vx2 += cf.y * dx * dx; vy2 += cf.y * dy * dy; vz2 += cf.y * dz * dz;
     }
     d.cg_b[i] = make_float4(vi.x + st_scale * bx, vi.y + st_scale * by, vi.z + st_scale * bz, 0.0f);
     d.cg_x[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
+    if (p.visc_solver == 1) {
+        // diag(A_0 + f I) per component; a non-positive entry is replaced by 1 + f and flagged in w
+        const float f1 = 1.0f + p.cg_factor;
+        float4 D = make_float4(f1 + p.dt * (csum - vx2), f1 + p.dt * (csum - vy2), f1 + p.dt * (csum - vz2), 0.0f);
+        int mask = 0;
+        if (!(D.x > 1.0e-6f)) { D.x = f1; mask |= 1; }
+        if (!(D.y > 1.0e-6f)) { D.y = f1; mask |= 2; }
+        if (!(D.z > 1.0e-6f)) { D.z = f1; mask |= 4; }
+        D.w = float(mask);
+        d.jac_d[i] = D;
+    }
 }
 
 // (A q)_i = q_i (1 + f) + dt [sum_j c_ij (q_i - q_j) - sum_j cv_ij ((q_i - q_j).x_ij) x_ij]
@@ -824,6 +842,71 @@ __global__ void __launch_bounds__(BS) k_cg_dir(Dev d, Params p, unsigned long lo
     d.cg_p[i] = q;
 }
 
+// One Jacobi sweep: r = b + f x0 - (A_0 + f I) q, q' = q + r / D, with r.r of the input iterate
+// reduced per scene for the stop test (r.r < cg_tol, as the CG's, MPSSolver.cuh:33-41).  The
+// iterates alternate between cg_x (even) and cg_p (odd) by the scene's loop counter, so that one
+// launch per sweep suffices; src/dst given = explicit buffers (adjoint recording).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long long cond, int use_cond, int limit,
+                                               const float4* src, float4* dst) {
+    __shared__ double sh[32];
+    __shared__ double2 sh2[BS / 32];
+    if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int s = block_scene(d, BS);
+    if (use_cond != 2 && !d.solve[s].active) return;
+    const Scene& sc = d.scenes[s];
+    const int l = d.solve[s].iter;
+    const float4* q = src ? src : (((l - 1) & 1) ? d.cg_p : d.cg_x);
+    float4* qn = dst ? dst : ((l & 1) ? d.cg_p : d.cg_x);
+    const int i = blockIdx.x * BS + threadIdx.x;
+    float rr = 0.0f;
+    if (i < sc.slot_begin + sc.n) {
+        const float3 a = apply_A(d, p, i, q, p.cg_factor);
+        const float4 b = d.cg_b[i];
+        const float4 v0 = d.vel[i];
+        const float4 qi = q[i];
+        const float4 D = d.jac_d[i];
+        const float f = p.cg_factor;
+        const float rx = b.x + f * v0.x - a.x, ry = b.y + f * v0.y - a.y, rz = b.z + f * v0.z - a.z;
+        rr = rx * rx + ry * ry + rz * rz;
+        qn[i] = make_float4(qi.x + rx / D.x, qi.y + ry / D.y, qi.z + rz / D.z, 0.0f);
+    }
+    const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
+    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
+    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
+    const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
+    if (threadIdx.x == 0) {
+        SceneSolve& S = d.solve[s];
+        const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
+        const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
+        S.err = trr;
+        S.rr = trr;
+        if (stop) {
+            S.active = 0;
+            S.do_update = 0;
+        } else {
+            S.do_update = 1;
+            S.iter = l + 1;
+            if (l + 1 > cap) S.active = 0;
+        }
+        finish_scene_decision(d, p, cond, use_cond);
+    }
+}
+
+// v = the Jacobi result: the iterate of loop counter l - 1 (buffer (l - 1) & 1), or src.
+__global__ void k_jacobi_finish(Dev d, Params p, const float4* src) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    const int s = d.chunk_scene[i / kChunk];
+    const Scene& sc = d.scenes[s];
+    if (i >= sc.slot_begin + sc.n) return;
+    const float4* q = src ? src : (((d.solve[s].iter - 1) & 1) ? d.cg_p : d.cg_x);
+    const float4 x = q[i];
+    float4 v = d.vel[i];
+    v.x = x.x; v.y = x.y; v.z = x.z;
+    d.vel[i] = v;
+}
+
 // v = x (copy predictVel back, MPSSPHNonPressureUtil.cu:177-180).
 __global__ void k_cg_finish(Dev d, Params p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -837,9 +920,14 @@ __global__ void k_cg_finish(Dev d, Params p) {
 }
 
 // ------------------------------------------------------------------ advection
-__device__ __forceinline__ float collide(float pos, float lo, float hi, float v) {
-    if (pos < lo && v < 0.0f) return fabsf(v) < 1.0e-4f ? 0.0f : -v * 0.4f;
-    if (pos > hi && v > 0.0f) return fabsf(v) < 1.0e-4f ? 0.0f : -v * 0.4f;
+// code: 0 unchanged, 1 reflected (-0.4 v), 2 stopped (|v| < 1e-4).
+__device__ __forceinline__ float collide(float pos, float lo, float hi, float v, unsigned& code) {
+    if ((pos < lo && v < 0.0f) || (pos > hi && v > 0.0f)) {
+        if (fabsf(v) < 1.0e-4f) { code = 2u; return 0.0f; }
+        code = 1u;
+        return -v * 0.4f;
+    }
+    code = 0u;
     return v;
 }
 
@@ -850,12 +938,14 @@ __global__ void k_advect(Dev d, Params p) {
     if (i >= sc.slot_begin + sc.n) return;
     float4 x = d.pos[i];
     float4 v = d.vel[i];
-    v.x = collide(x.x + v.x * p.dt, sc.bminx, sc.bmaxx, v.x);
-    v.y = collide(x.y + v.y * p.dt, sc.bminy, sc.bmaxy, v.y);
-    v.z = collide(x.z + v.z * p.dt, sc.bminz, sc.bmaxz, v.z);
+    unsigned cx, cy, cz;
+    v.x = collide(x.x + v.x * p.dt, sc.bminx, sc.bmaxx, v.x, cx);
+    v.y = collide(x.y + v.y * p.dt, sc.bminy, sc.bmaxy, v.y, cy);
+    v.z = collide(x.z + v.z * p.dt, sc.bminz, sc.bmaxz, v.z, cz);
     x.x += p.dt * v.x; x.y += p.dt * v.y; x.z += p.dt * v.z;
     d.pos[i] = x;
     d.vel[i] = v;
+    if (d.tape_adv) d.tape_adv[i] = (unsigned char)(cx | (cy << 2) | (cz << 4));
 }
 
 // Loads a state given in particle-ID order (pos4.w = particle radius) into the slot layout.
@@ -961,6 +1051,13 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 void launch_cg_dir(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_dir, d, p, cond, use_cond, limit);
+}
+void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                   const float4* src, float4* dst, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_jacobi, d, p, cond, use_cond, limit, src, dst);
+}
+void launch_jacobi_finish(const Dev& d, const Params& p, const float4* src, cudaStream_t s) {
+    k_jacobi_finish<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p, src);
 }
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s) {
     k_cg_finish<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);

@@ -91,6 +91,8 @@ class Simulation:
         self.h = h
         self.n = 0
         self.nb = 0
+        self.nscenes = 1
+        self.material = dict(material)
 
     @classmethod
     def from_scene(cls, scene: Scene, device: int = 0, **config) -> "Simulation":
@@ -162,6 +164,12 @@ class Simulation:
         L.check(self.lib.mps_get_grid(self.h, o, C.byref(c), d))
         return dict(origin=tuple(o), cell=c.value, dims=tuple(d))
 
+    def set_material(self, **changes) -> None:
+        """Updates material constants (e.g. viscosity, surface_tension); graphs are re-captured."""
+        self.material.update(changes)
+        m = _material(self.material)
+        L.check(self.lib.mps_set_material(self.h, C.byref(m)))
+
     # ------------------------------------------------------------------ stepping
     def step(self, nsteps: int = 1, stream=None) -> None:
         L.check(self.lib.mps_step(self.h, nsteps, _stream(stream)))
@@ -200,8 +208,10 @@ class Simulation:
         """Kernel launches of one graph step given its loop-body counts (DF, CG, CD)."""
         # keys + radix (3 per pass) + reorder, lists, [volume], density, DF init + condition
         static = 2 + 3 * radix_passes + 1 + (1 if self.cfg.volume_accumulate else 0) + 1 + 2
-        static += 6 + 4 + 2  # DF finish + CG set-up, CG finish + CD set-up, CD finish + advect
-        return static + 2 * runs[0] + 3 * runs[1] + 2 * runs[2]
+        jacobi = self.cfg.visc_solver == L.VISC_JACOBI
+        # DF finish + solve set-up (+ A x0 for the CG), solve finish + CD set-up, CD finish + advect
+        static += (5 if jacobi else 6) + 4 + 2
+        return static + 2 * runs[0] + (1 if jacobi else 3) * runs[1] + 2 * runs[2]
 
 
 class BatchedSimulation(Simulation):
@@ -227,6 +237,7 @@ class BatchedSimulation(Simulation):
                                             fo.ctypes.data_as(C.c_void_p), bo.ctypes.data_as(C.c_void_p),
                                             boxes.ctypes.data_as(C.c_void_p), C.byref(h)))
         self.h = h
+        self.material = dict(base.material)
         self.n = int(fo[-1])
         self.nb = int(bo[-1])
         self.offsets = fo

@@ -538,6 +538,74 @@ double dot3n(const std::vector<d3>& a, const std::vector<d3>& b) {
     return s;
 }
 
+// Diagonal of A_0 + f I per component: (1 + f) + dt [sum_j (ST + XSPH coefficient) -
+// sum_j (viscosity coefficient) x_ij,c^2], the coefficients of cg_apply's terms; a non-positive
+// entry is replaced by 1 + f.
+void jacobi_diag(const orc_sim& s, std::vector<d3>& D, double factor) {
+    const int64_t n = s.n;
+    const double dt = s.p.dt;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const double hi = s.radius[size_t(i)] * kHRatio;
+        const double invHi = 1.0 / hi;
+        const d3 xi = s.pos[size_t(i)];
+        const double mi = s.mass[size_t(i)], di = s.density[size_t(i)];
+        double cst = 0.0, cx = 0.0;
+        d3 cv{0, 0, 0};
+        for_nei(s.ff, i, [&](uint32_t jd) {
+            const d3 xij = xi - s.pos[jd];
+            const double dist = length(xij);
+            const double mij = 0.5 * (mi + s.mass[jd]);
+            cst += mij * st_gij(s, i, jd, xij, dist, invHi);
+            cx += (s.mass[jd] / s.density[jd]) * WKernel(dist, invHi, s.p.cubic);
+            const double c = 0.5 * (mi + s.mass[jd]) / s.density[jd] / (dist * dist + 0.01 * hi * hi) *
+                             GKernel(dist, invHi, s.p.cubic) / (dist + kFltEps);
+            cv += d3{c * xij.x * xij.x, c * xij.y * xij.y, c * xij.z * xij.z};
+        });
+        const double c0 = (dt * s.p.surface_tension / mi) * cst + (s.p.xsph / dt) * cx;
+        const double vs = 10.0 * s.p.mat_density * s.p.viscosity / di;
+        auto diag = [&](double cvc) {
+            const double v = (1.0 + factor) + dt * (c0 - vs * cvc);
+            return v > 1.0e-6 ? v : 1.0 + factor;
+        };
+        D[size_t(i)] = d3{diag(cv.x), diag(cv.y), diag(cv.z)};
+    }
+}
+
+// Point-Jacobi alternative of the CG on the same system: from x0 = v,
+// x += D^-1 (b + f x0 - (A_0 + f I) x) until r.r < cg_tol (at most cg_max_iter sweeps) or for
+// fixed_iters sweeps (the reference's legacy Jacobi viscosity, MPSSPHNonPressureUtil.cuh:90-195,
+// iterated a block-diagonal inverse on the viscosity term alone).
+int viscst_jacobi(orc_sim& s, double* rr_out) {
+    const int64_t n = s.n;
+    const double f = 0.01;   // the CG iterations' operator factor (MPSSPHNonPressureUtil.cu:165-169)
+    std::vector<d3> D(static_cast<size_t>(n)), Ax(static_cast<size_t>(n));
+    jacobi_diag(s, D, f);
+    std::vector<d3>& x = s.predict;
+    const std::vector<d3> x0 = s.vel;
+    int l = 1;
+    const int cap = s.p.fixed_iters > 0 ? s.p.fixed_iters : s.p.cg_max_iter;
+    while (l <= cap) {
+        cg_apply(s, x, Ax, f);
+        double rr = 0.0;
+        std::vector<d3> r(static_cast<size_t>(n));
+        for (int64_t i = 0; i < n; ++i) {
+            r[size_t(i)] = (s.cgb[size_t(i)] + f * x0[size_t(i)]) - Ax[size_t(i)];
+            rr += r[size_t(i)].x * r[size_t(i)].x;
+            rr += r[size_t(i)].y * r[size_t(i)].y;
+            rr += r[size_t(i)].z * r[size_t(i)].z;
+        }
+        *rr_out = rr;
+        if (s.p.fixed_iters <= 0 && rr < s.p.cg_tol) break;
+        for (int64_t i = 0; i < n; ++i) {
+            const d3 d = D[size_t(i)];
+            x[size_t(i)] += d3{r[size_t(i)].x / d.x, r[size_t(i)].y / d.y, r[size_t(i)].z / d.z};
+        }
+        l++;
+    }
+    return l;
+}
+
 // ApplyImplicitViscosityNSurfaceTension + CGSolver (MPSSPHNonPressureUtil.cu:127-188,
 // MPSSolver.cuh:12-73, MPSCGKernel.cuh:5-133).  The operator uses f = 0 for A x0 and
 // f = 0.01 for every iteration (:165-169).
@@ -548,6 +616,11 @@ int phase_viscst(orc_sim& s, double* rr_out) {
     s.predict = s.vel;
     st_factor(s);
     st_cgb(s);
+    if (s.p.visc_solver == 1) {
+        const int l = viscst_jacobi(s, rr_out);
+        s.vel = s.predict;
+        return l;
+    }
     std::vector<d3> r(static_cast<size_t>(n)), p(static_cast<size_t>(n)), Ap(static_cast<size_t>(n));
     std::vector<d3>& x = s.predict;
     cg_apply(s, x, Ap, 0.0);

@@ -25,7 +25,7 @@ class Params(C.Structure):
                 ("cubic", C.c_int32), ("df_tol", C.c_double), ("cd_tol", C.c_double), ("df_min_iter", C.c_int32),
                 ("cd_min_iter", C.c_int32), ("max_iter", C.c_int32), ("cg_tol", C.c_double),
                 ("cg_max_iter", C.c_int32), ("volume_accumulate", C.c_int32), ("zsort", C.c_int32),
-                ("threads", C.c_int32), ("fixed_iters", C.c_int32)]
+                ("threads", C.c_int32), ("fixed_iters", C.c_int32), ("visc_solver", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -109,6 +109,7 @@ def params(material: dict, physics: dict, config: dict | None = None, hash_cell:
     p.zsort = int(kw.get("zsort", 0))
     p.threads = int(kw.get("threads", 0))
     p.fixed_iters = int(cfg.get("fixed_iters", 0))
+    p.visc_solver = int(cfg.get("visc_solver", 0))
     return p
 
 
