@@ -310,6 +310,193 @@ def run_batched(args, scenes_list, rank, world, local_rank):
     return line
 
 
+def adjoint_launches(sim, K: int, nsteps: int, every: int, passes: int) -> int:
+    """Kernel launches of one forward + reverse: graph steps (forward and segment recompute), the
+    recorded eager step and the reverse kernels of every step."""
+    per_step = sim.launches_per_step((K, K, K), passes)
+    eager = per_step + 2          # recorded step: + solver init/finish around the Jacobi sweeps
+    reverse = 10 + 5 * K          # gather, index, collision, 2K CD, K Jacobi, set-up, ST factor, 2K DF, density x2, scatter, sums
+    nseg = (nsteps + every - 1) // every
+    return nsteps * per_step + (nsteps - nseg) * per_step + nsteps * (eager + reverse)
+
+
+def host_gradient_baseline(scene, steps: int = 1):
+    """FP64 torch reverse-mode of the same step on the host cores (the checker's restatement)."""
+    import numpy as np
+    import torch
+    from oracle import adjoint_ref as A
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    R = A.RefScene(scene.pos4, scene.vel4, scene.bpos4, scene.material, scene.physics, True,
+                   int(scene.config["fixed_iters"]))
+    rng = np.random.default_rng(0)
+    gx, gv = rng.normal(size=(scene.n, 3)), rng.normal(size=(scene.n, 3))
+    t0 = time.perf_counter()
+    A.gradient(R, steps, gx, gv)
+    dt = time.perf_counter() - t0
+    return {"value": scene.n * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} step(s) forward + reverse of one {scene.name} scene ({scene.n} fluid), FP64 torch "
+                      f"autograd of the restated step on the host cores, {dt:.1f} s"}
+
+
+def fd_check(scene, horizon: int, every: int, device: int):
+    """GPU gradient of the centre-of-mass loss against FP64 central differences of the C++ oracle
+    (eps = 1e-4 relative) for one scene over `horizon` steps: directional derivative along a
+    seeded v0 direction, d/dviscosity, d/dsurface_tension."""
+    import numpy as np
+    import torch
+    from mps_cuda_gb300 import Simulation
+    from mps_cuda_gb300.adjoint import AdjointRollout, com_loss
+    from oracle import oracle as O
+    target = np.array(scene.meta["target"], np.float64)
+    m = scene.vel4[:, 3].astype(np.float64)
+
+    def loss_np(x, v):
+        com = (m[:, None] * x).sum(0) / m.sum()
+        return float(((com - target) ** 2).sum() + 1e-3 * (v * v).sum(1).mean())
+
+    sim = Simulation.from_scene(scene, device=device)
+    roll = AdjointRollout(sim, horizon, every)
+    pT, vT = roll.forward()
+    xT = torch.tensor(pT[:, :3], dtype=torch.float64, requires_grad=True)
+    vTt = torch.tensor(vT[:, :3], dtype=torch.float64, requires_grad=True)
+    com_loss(xT, vTt, torch.tensor(m), [0, scene.n], torch.tensor(target[None, :])).sum().backward()
+    g4x = np.zeros((scene.n, 4), np.float32)
+    g4v = np.zeros((scene.n, 4), np.float32)
+    g4x[:, :3] = xT.grad.numpy()
+    g4v[:, :3] = vTt.grad.numpy()
+    _, ov, par = roll.backward(g4x, g4v)
+    sim.close()
+    cfg = dict(scene.config, visc_solver=1)
+    threads = os.cpu_count() or 1
+    v0 = scene.vel4[:, :3].astype(np.float64)
+    u = np.random.default_rng(1234).normal(size=v0.shape)
+
+    def oracle_loss(vel=None, **mat):
+        sc_mat = dict(scene.material, **mat)
+        o = O.Oracle(O.params(sc_mat, scene.physics, cfg, hash_size=tuple(
+            int(2 ** np.ceil(np.log2(max(4, e / sc_mat["radius"] * 2 + 4))))
+            for e in np.asarray(scene.physics["max"]) - np.asarray(scene.physics["min"])), threads=threads))
+        o.set_boundary(scene.bpos4[:, :3].astype(np.float64), scene.bpos4[:, 3].astype(np.float64))
+        o.set_fluid(scene.pos4[:, :3].astype(np.float64), v0 if vel is None else vel, m,
+                    scene.pos4[:, 3].astype(np.float64))
+        o.step(horizon)
+        return loss_np(o.get("pos"), o.get("vel"))
+
+    out = {"horizon": horizon, "scene": scene.name, "eps_relative": 1e-4}
+    eps = 1e-4 * np.abs(v0).max()
+    fd = (oracle_loss(vel=v0 + eps * u) - oracle_loss(vel=v0 - eps * u)) / (2 * eps)
+    ad = float((ov[:, :3].astype(np.float64) * u).sum())
+    out["v0_direction"] = {"fd": fd, "adjoint": ad, "rel_err": abs(ad - fd) / abs(fd)}
+    for k, name in ((0, "viscosity"), (1, "surface_tension")):
+        val = float(scene.material[name])
+        e = 1e-4 * val
+        fd = (oracle_loss(**{name: val + e}) - oracle_loss(**{name: val - e})) / (2 * e)
+        out[name] = {"fd": fd, "adjoint": float(par[0, k]), "rel_err": abs(float(par[0, k]) - fd) / abs(fd)}
+    return out
+
+
+def run_adjoint(args, rank, world, local_rank):
+    """Forward + reverse of the 200-step rollout of 32 seeded 16k-particle scenes (one batched
+    handle), gradients of the centre-of-mass loss w.r.t. v0, viscosity and surface tension."""
+    import numpy as np
+    import torch
+    from mps_cuda_gb300 import BatchedSimulation, build, scenes
+    from mps_cuda_gb300.adjoint import AdjointRollout, com_loss, rollout
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    scs = scenes.adjoint_scenes(32, seed=rank)
+    horizon = args.steps
+    every = 20
+    K = int(scs[0].config["fixed_iters"])
+    sim = BatchedSimulation(scs, device=local_rank)
+    n = sim.n
+    mass = torch.tensor(np.concatenate([s.vel4[:, 3] for s in scs]), dtype=torch.float64)
+    targets = torch.tensor([s.meta["target"] for s in scs], dtype=torch.float64)
+    p0, v0 = sim.get_fluid()
+
+    def cotangents(pT, vT):
+        xT = torch.tensor(pT[:, :3], dtype=torch.float64, requires_grad=True)
+        vTt = torch.tensor(vT[:, :3], dtype=torch.float64, requires_grad=True)
+        L = com_loss(xT, vTt, mass, sim.offsets, targets)
+        L.sum().backward()
+        g4x = np.zeros((n, 4), np.float32)
+        g4v = np.zeros((n, 4), np.float32)
+        g4x[:, :3] = xT.grad.numpy()
+        g4v[:, :3] = vTt.grad.numpy()
+        return L.detach().numpy(), g4x, g4v
+
+    # warm-up: a short rollout forward + reverse (graph capture, buffers)
+    warm = AdjointRollout(sim, args.warmup, min(every, args.warmup))
+    pT, vT = warm.forward(p0, v0)
+    warm.backward(*cotangents(pT, vT)[1:])
+    roll = AdjointRollout(sim, horizon, every)
+    roll.reserve()
+    torch.cuda.synchronize(dev)
+    e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    with ClockSampler(local_rank) as clk:
+        sim.set_fluid(p0, v0)
+        e0.record(stream)
+        L_check = roll.lib.mps_adjoint_forward(sim.h, horizon, every, None)
+        e1.record(stream)
+        e1.synchronize()
+        pT, vT = sim.get_fluid()
+        loss, g4x, g4v = cotangents(pT, vT)
+        e2.record(stream)
+        op, ov, par = roll.backward(g4x, g4v)
+        e3.record(stream)
+        e3.synchronize()
+    assert L_check == 0
+    fwd_ms, bwd_ms = e0.elapsed_time(e1), e2.elapsed_time(e3)
+    total_ms = fwd_ms + bwd_ms
+    value = n * horizon / (total_ms / 1e3)
+    # e2e: the torch.autograd harness with host tensors (state H2D, rollout, D2H, loss, reverse)
+    x0 = torch.tensor(p0[:, :3], dtype=torch.float64, requires_grad=True)
+    v0t = torch.tensor(v0[:, :3], dtype=torch.float64, requires_grad=True)
+    mu = torch.tensor(scs[0].material["viscosity"], dtype=torch.float64, requires_grad=True)
+    sg = torch.tensor(scs[0].material["surface_tension"], dtype=torch.float64, requires_grad=True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    xT, vTt = rollout(roll, x0, v0t, mu, sg)
+    com_loss(xT, vTt, mass, sim.offsets, targets).sum().backward()
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    same = bool(np.allclose(v0t.grad.numpy(), ov[:, :3], rtol=0, atol=0))
+    line = {
+        "metric": "particle-steps/s (DFSPH adjoint: forward + reverse, 32 x 16k scenes)", "value": value,
+        "unit": UNIT, "n_gpus": world, "steps": horizon, "warmup": args.warmup,
+        "ms_per_step": total_ms / horizon, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "adjoint_16k", "scenes": len(scs), "fluid_particles": n, "boundary_particles": sim.nb,
+                   "fixed_iters": K, "visc_solver": "jacobi", "checkpoint_every": every, "horizon": horizon,
+                   "loss": "|COM_T - target|^2 + 1e-3 mean |v_T|^2 per scene",
+                   "l2": "inputs larger than L2: per-step tape ~%.0f MB > 129 MB" % (roll.memory_bytes() / 1e6)},
+        "forward": {"ms": fwd_ms, "particle_steps_per_s": n * horizon / (fwd_ms / 1e3)},
+        "reverse": {"ms": bwd_ms, "particle_steps_per_s": n * horizon / (bwd_ms / 1e3)},
+        "adjoint_memory_bytes": roll.memory_bytes(),
+        "loss_mean": float(np.mean(loss)),
+        "grad": {"v0_norm": float(np.linalg.norm(ov[:, :3])), "d_viscosity_mean": float(par[:, 0].mean()),
+                 "d_surface_tension_mean": float(par[:, 1].mean()), "finite": bool(np.isfinite(ov).all() and np.isfinite(par).all())},
+        "roofline": None,
+        "roofline_note": "per-kernel HBM roofline is reported by the plain-step line (dam_break_1m)",
+        "e2e": {"value": n * horizon / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (32 * n + 32 * n) / horizon,
+                "d2h_bytes_per_step": (32 * n + 32 * n + 32 * n) / horizon,
+                "note": "torch.autograd.Function over the C ABI: initial state in, final state out, cotangents in, "
+                        "gradients out, host loss; bytes amortised over the horizon", "same_gradient": same},
+        "gpu_launches": adjoint_launches(sim, K, horizon, every, radix_passes(sim)),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = host_gradient_baseline(scs[0], 1)
+    if args.check:
+        line["gradient_check"] = [fd_check(scs[k], args.check_steps, min(every, args.check_steps), local_rank)
+                                  for k in range(args.check_scenes)]
+    sim.close()
+    return line
+
+
 def run_reference(args, scene, rank, world, local_rank):
     """The reference's own CUDA step (FP64) on rank 0."""
     if rank != 0:
@@ -351,7 +538,7 @@ def run_reference(args, scene, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (adjoint_16k: the rollout horizon, 200)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="dam_break_1m")
@@ -359,10 +546,21 @@ def main():
     ap.add_argument("--eager", action="store_true",
                     help="host-driven solver loops instead of the CUDA graph (same kernels; for ncu, which "
                          "cannot profile kernels of graphs with conditional nodes)")
+    ap.add_argument("--check", action="store_true",
+                    help="adjoint_16k: also check the gradient against FP64 central differences of the oracle")
+    ap.add_argument("--check-steps", type=int, default=20)
+    ap.add_argument("--check-scenes", type=int, default=1)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.steps is None:
+        args.steps = 200 if args.config == "adjoint_16k" else 10
     rank, world, local_rank = env_rank()
     from mps_cuda_gb300 import scenes
+    if args.config == "adjoint_16k" and args.impl == "ours":
+        line = run_adjoint(args, rank, world, local_rank)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     if args.config == "batched_256":
         line = run_batched(args, scenes.batched_scenes(256, seed=0), rank, world, local_rank)
         if rank == 0:

@@ -86,12 +86,13 @@ typedef struct mps_config {
     int32_t visc_solver;         /* mps_visc_solver: implicit viscosity/surface-tension solve */
 } mps_config;
 
-/* MPS_VISC_CG: the reference's CGSolver (MPSSolver.cuh:12-73).  MPS_VISC_JACOBI: point-Jacobi
+/* MPS_VISC_CG: the reference's CGSolver (MPSSolver.cuh:12-73).  MPS_VISC_JACOBI: block-Jacobi
  * sweeps on the same system, the alternative of the reference's legacy Jacobi viscosity
- * (MPSSPHNonPressureUtil.cuh:90-195, commented out there).  The CG's converged point satisfies
- * (A_0 + f I) x = b + f x0 (f = cg_factor, x0 = pre-solve velocity); Jacobi iterates
- * x += D^-1 (b + f x0 - (A_0 + f I) x), D = diag(A_0 + f I), from x0, stopping when the residual's
- * r.r < cg_tol (at most cg_max_iter sweeps) or after fixed_iters sweeps. */
+ * (MPSSPHNonPressureUtil.cuh:90-195, commented out there, which also inverts each particle's 3x3
+ * block).  The CG's converged point satisfies (A_0 + f I) x = b + f x0 (f = cg_factor, x0 =
+ * pre-solve velocity); Jacobi iterates x += D^-1 (b + f x0 - (A_0 + f I) x), D = the 3x3 diagonal
+ * blocks of A_0 + f I, from x0, stopping when the residual's r.r < cg_tol (at most cg_max_iter
+ * sweeps) or after fixed_iters sweeps. */
 enum mps_visc_solver { MPS_VISC_CG = 0, MPS_VISC_JACOBI = 1 };
 
 /* Per-step statistics, written by the device at the end of each step. */
@@ -258,6 +259,8 @@ int mps_adjoint_backward(mps_handle* h, const float* g_pos4, const float* g_vel4
                          float* g_vel0, double* g_param2, void* stream);
 /* Device bytes the adjoint holds for the current layout (checkpoints + one step's tape). */
 int64_t mps_adjoint_memory(mps_handle* h, int32_t nsteps, int32_t checkpoint_every);
+/* Allocates those buffers now (mps_adjoint_forward otherwise allocates on first use). */
+int mps_adjoint_reserve(mps_handle* h, int32_t nsteps, int32_t checkpoint_every);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -102,6 +102,7 @@ EXPORTS = {
     "mps_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "mps_adjoint_memory": (C.c_int64, [C.c_void_p, C.c_int32, C.c_int32]),
+    "mps_adjoint_reserve": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
 }
 
 _lib = None

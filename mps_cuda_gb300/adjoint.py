@@ -38,14 +38,18 @@ class AdjointRollout:
     def memory_bytes(self) -> int:
         return int(self.lib.mps_adjoint_memory(self.sim.h, self.nsteps, self.every))
 
+    def reserve(self) -> None:
+        """Allocates the checkpoint and tape buffers now (else on the first forward)."""
+        L.check(self.lib.mps_adjoint_reserve(self.sim.h, self.nsteps, self.every))
+
     def forward(self, pos4: np.ndarray | None = None, vel4: np.ndarray | None = None, visc: float | None = None,
                 sigma: float | None = None, stream=None) -> tuple[np.ndarray, np.ndarray]:
         """Sets the initial state / coefficients (when given), runs the recorded forward, returns
         the final state (ID order, float32 (N, 4))."""
         changes = {}
-        if visc is not None:
+        if visc is not None and float(visc) != self.sim.material["viscosity"]:
             changes["viscosity"] = float(visc)
-        if sigma is not None:
+        if sigma is not None and float(sigma) != self.sim.material["surface_tension"]:
             changes["surface_tension"] = float(sigma)
         if changes:
             self.sim.set_material(**changes)

@@ -10,7 +10,8 @@
 //            kappa_i = max(0, min(dt delta_i, rho_i/rho0 + dt delta_i - 0.8)) alpha_i / dt^2,
 //            u_i    += -dt [0.5 V sum_j (kappa_i + kappa_j) G_ij x_ij + 0.5 kappa_i sum_b Vb G_ib x_ib]
 //   viscosity + surface tension + XSPH: coefficients c_ij, cv_ij, b_i from (x, v, rho, st factor)
-//            (k_cg_b), then K Jacobi sweeps q += D^-1 (b + f x0 - (A_0 + f I) q) from q = x0 = v
+//            (k_cg_b), then K block-Jacobi sweeps q += D^-1 (b + f x0 - (A_0 + f I) q) from
+//            q = x0 = v, D = each particle's 3x3 diagonal block
 //   K x CD:  as DF with kappa_i = max(0, rho_i/rho0 + dt delta_i - 1) alpha_i / dt^2
 //   collision (per axis: v, -0.4 v or 0) and x += dt v.
 // Neighbour sets are piecewise constant in x (no derivative).  Every pair term's reverse is
@@ -18,7 +19,8 @@
 // its list) and of the terms its neighbours own (pairs (j, i), found through the reverse index
 // rev[k][i] = position of i in j's list), so each cotangent is written by one thread and the
 // result is deterministic.  The Jacobi solve reverses exactly as K transposed sweeps
-// y = qbar / D, qbar -= (A_0 + f I)^T y.
+// y = D^-1 qbar, qbar -= (A_0 + f I)^T y (D symmetric).  A pair whose reverse entry is missing
+// (asymmetric lists, only after a capacity overflow) is skipped and the call reports it.
 //
 // Memory: checkpoints of the slot-order state every `every` steps, the start states of one
 // segment, and one step's tape (K + 1 velocity fields per pressure solve, K + 1 Jacobi iterates,
@@ -60,8 +62,10 @@ struct AdjointStore {
     unsigned char *t_cdf = nullptr, *t_ccd = nullptr, *t_adv = nullptr;
     // cotangents
     float4 *gx = nullptr, *gv = nullptr, *gx_id = nullptr, *gv_id = nullptr;
-    float4 *qbar0 = nullptr, *qbar1 = nullptr, *bbar = nullptr, *Dbar = nullptr, *gg = nullptr;
-    float *grho = nullptr, *galpha = nullptr, *gdelta = nullptr, *gsf = nullptr, *gsig = nullptr, *gmu = nullptr;
+    float4 *qbar0 = nullptr, *qbar1 = nullptr, *bbar = nullptr, *gg = nullptr;
+    float4 *Dbar = nullptr, *Dbar2 = nullptr;   // symmetric 3x3 cotangent of the Jacobi block: (xx, yy, zz, xy), (xz, yz)
+    float *grho = nullptr, *galpha = nullptr, *gdelta = nullptr, *gsf = nullptr;
+    double *gsig = nullptr, *gmu = nullptr;   // per-slot parameter cotangents (FP64)
     float2* pc = nullptr;            // per pair (cbar, cvbar), interleaved like nbr_f
     float4* px = nullptr;            // per pair explicit x_ij cotangent
     unsigned char* rev = nullptr;    // per pair: position of i in the neighbour's list
@@ -72,7 +76,7 @@ struct AdjointStore {
     void free_all() {
         void* ptrs[] = {cp_pos, cp_vel, cp_ids, fin_pos, fin_vel, fin_ids, seg_pos, seg_vel, seg_ids, t_udf, t_ucd,
                         t_q, t_x, t_kdf, t_kcd, t_cdf, t_ccd, t_adv, gx, gv, gx_id, gv_id, qbar0, qbar1, bbar,
-                        Dbar, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
+                        Dbar, Dbar2, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         *this = AdjointStore{};
@@ -90,7 +94,11 @@ __device__ __forceinline__ float3 operator*(float s, float3 a) { return make_flo
 __device__ __forceinline__ float3& operator+=(float3& a, float3 b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
 __device__ __forceinline__ float3& operator-=(float3& a, float3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; return a; }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float3 mul3(float3 a, float3 b) { return make_float3(a.x * b.x, a.y * b.y, a.z * b.z); }
+// symmetric 3x3 stored as (xx, yy, zz, xy) + (xz, yz)
+__device__ __forceinline__ float3 sym_mul(float4 m, float4 m2, float3 v) {
+    return make_float3(m.x * v.x + m.w * v.y + m2.x * v.z, m.w * v.x + m.y * v.y + m2.y * v.z,
+                       m2.x * v.x + m2.y * v.y + m.z * v.z);
+}
 
 // Kernel values and radial derivatives at distance r: W, dW/dr, G (grad W = G x), dG/dr.
 // Same piecewise forms as kW / kG (MPSSPHKernel.cuh:28-65), differentiated per piece.
@@ -340,17 +348,16 @@ __global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X
 // the cotangents of b, D and of each pair's coefficients (c, cv) and explicit x_ij.
 __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float4* X, const unsigned char* rev,
                                                      const float4* qk, const float4* qk1, const float4* qbar,
-                                                     float4* qbar_out, float4* bbar, float4* Dbar, float2* pc,
-                                                     float4* px) {
+                                                     float4* qbar_out, float4* bbar, float4* Dbar, float4* Dbar2,
+                                                     float2* pc, float4* px) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.slots) return;
     int s;
     if (!slot_live(d, i, s)) return;
     const size_t S = size_t(p.slots);
     const float4 xi = X[i];
-    const float4 Di = d.jac_d[i];
     const float4 qb = qbar[i];
-    const float3 y = make_float3(qb.x / Di.x, qb.y / Di.y, qb.z / Di.z);
+    const float3 y = sym_mul(d.jac_d[i], d.jac_d2[i], f3(qb));
     const float3 qi = f3(qk[i]);
     const int nf = int(d.cnt[i] & 0xffffu);
     float3 aty = (1.0f + p.cg_factor) * y;
@@ -358,14 +365,17 @@ __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float
         const size_t at = size_t(k) * S + size_t(i);
         const unsigned j = d.nbr_f[at];
         const float2 cij = d.cg_coef[at];
-        const float2 cji = d.cg_coef[size_t(rev[at]) * S + j];
-        const float4 Dj = d.jac_d[j];
-        const float4 qbj = qbar[j];
-        const float3 yj = make_float3(qbj.x / Dj.x, qbj.y / Dj.y, qbj.z / Dj.z);
         const float4 xj = X[j];
         const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-        const float ye = dot3(y, e), yje = dot3(yj, e);
-        aty += p.dt * ((cij.x * y - (cij.y * ye) * e) - (cji.x * yj - (cji.y * yje) * e));
+        const float ye = dot3(y, e);
+        aty += p.dt * (cij.x * y - (cij.y * ye) * e);
+        const unsigned rv = rev[at];
+        if (rv != 255u) {
+            const float2 cji = d.cg_coef[size_t(rv) * S + j];
+            const float3 yj = sym_mul(d.jac_d[j], d.jac_d2[j], f3(qbar[j]));
+            const float yje = dot3(yj, e);
+            aty -= p.dt * (cji.x * yj - (cji.y * yje) * e);
+        }
         const float3 pp = qi - f3(qk[j]);
         const float pe = dot3(pp, e);
         float2 a = pc[at];
@@ -381,10 +391,16 @@ __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float
     float4 bb = bbar[i];
     bb.x += y.x; bb.y += y.y; bb.z += y.z;
     bbar[i] = bb;
+    // Dbar -= sym(y dq^T), dq = q^{k+1} - q^k = D^-1 r
     const float3 dq = f3(qk1[i]) - qi;
     float4 db = Dbar[i];
     db.x -= y.x * dq.x; db.y -= y.y * dq.y; db.z -= y.z * dq.z;
+    db.w -= 0.5f * (y.x * dq.y + y.y * dq.x);
     Dbar[i] = db;
+    float4 db2 = Dbar2[i];
+    db2.x -= 0.5f * (y.x * dq.z + y.z * dq.x);
+    db2.y -= 0.5f * (y.y * dq.z + y.z * dq.y);
+    Dbar2[i] = db2;
 }
 
 // Inputs of one pair term of the solve set-up (k_cg_b), owner o, neighbour n.
@@ -403,7 +419,8 @@ struct PairBar {
 };
 struct PairGrad {
     float3 e, vo, vn;
-    float ro, rn, so, sn, sig, mu;
+    float ro, rn, so, sn;
+    double sig, mu;    // parameter cotangents: small totals of cancelling terms, kept in FP64
 };
 
 // Reverse of the pair term: c = mbar g_on, b share = -st_scale c e,
@@ -436,20 +453,21 @@ __device__ PairGrad pair_reverse(const Params& p, const PairIn& in, const PairBa
     float rbar = 0.0f;
     float3 ebar = bar.X;
     // cv
-    g.mu = bar.Cv * vs0 * kd.G / (den * rr);
+    g.mu = double(bar.Cv) * double(vs0) * double(kd.G) / (double(den) * double(rr));
     g.ro = -bar.Cv * cv / in.ro;
     g.rn = -bar.Cv * cv / in.rn;
     rbar += bar.Cv * p.visc * vs0 * (kd.dG / (den * rr) - kd.G * 2.0f * r / (den * den * rr) - kd.G / (den * rr * rr));
     // c_on
     float cbar = bar.C * st_scale;
-    g.sig = bar.C * (p.dt / in.mo) * c;
+    const double dtm = double(p.dt) / double(in.mo);
+    g.sig = double(bar.C) * dtm * double(c);
     g.rn += -bar.C * xs * in.mn * kd.W / (in.rn * in.rn);
     rbar += bar.C * xs * (in.mn / in.rn) * kd.dW;
     // b share: st_scale * (-c e)
     const float3 Bt = st_scale * bar.Bb;
     cbar += -dot3(Bt, in.e);
     ebar -= c * Bt;
-    g.sig += -(p.dt / in.mo) * c * dot3(bar.Bb, in.e);
+    g.sig -= dtm * double(c) * (double(bar.Bb.x) * in.e.x + double(bar.Bb.y) * in.e.y + double(bar.Bb.z) * in.e.z);
     // c = mbar g; g = E invD
     const float gbar = cbar * mbar;
     const float Ebar = gbar * invD;
@@ -478,9 +496,9 @@ __device__ PairGrad pair_reverse(const Params& p, const PairIn& in, const PairBa
 // into x, the pre-solve velocity, rho, the ST factor and the per-particle sigma / mu shares.
 __global__ void __launch_bounds__(kAB) k_adj_visc_coef(Dev d, Params p, const float4* X, const float4* V0,
                                                         const unsigned char* rev, const float4* qbar0,
-                                                        const float4* bbar, const float4* Dbar, const float2* pc,
-                                                        const float4* px, float4* gv, float4* gx, float* grho,
-                                                        float* gsf, float* gsig, float* gmu) {
+                                                        const float4* bbar, const float4* Dbar, const float4* Dbar2,
+                                                        const float2* pc, const float4* px, float4* gv, float4* gx,
+                                                        float* grho, float* gsf, double* gsig, double* gmu) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.slots) return;
     int s;
@@ -490,15 +508,15 @@ __global__ void __launch_bounds__(kAB) k_adj_visc_coef(Dev d, Params p, const fl
     const float4 vi4 = V0[i];
     const float2 ai = d.aux[i];
     const float4 bbi = bbar[i];
-    const float4 Di = d.jac_d[i];
-    const int mi = int(Di.w);
-    const float4 Dbi4 = Dbar[i];
-    const float3 Dbi = make_float3(mi & 1 ? 0.f : Dbi4.x, mi & 2 ? 0.f : Dbi4.y, mi & 4 ? 0.f : Dbi4.z);
+    const bool keep_i = d.jac_d2[i].z == 0.0f;   // a replaced block does not depend on the coefficients
+    const float4 Dbi = keep_i ? Dbar[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 Dbi2 = keep_i ? Dbar2[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int nf = int(d.cnt[i] & 0xffffu);
     float3 gvi = f3(qbar0[i]) + (1.0f + p.cg_factor) * f3(bbi);
     float3 gxi = make_float3(0.f, 0.f, 0.f);
-    float grhoi = 0.0f, gsfi = 0.0f, sig = 0.0f, mu = 0.0f;
-    const float dsumi = Dbi.x + Dbi.y + Dbi.z;
+    float grhoi = 0.0f, gsfi = 0.0f;
+    double sig = 0.0, mu = 0.0;
+    const float tri = Dbi.x + Dbi.y + Dbi.z;
     for (int k = 0; k < nf; ++k) {
         const size_t at = size_t(k) * S + size_t(i);
         const unsigned j = d.nbr_f[at];
@@ -506,7 +524,9 @@ __global__ void __launch_bounds__(kAB) k_adj_visc_coef(Dev d, Params p, const fl
         const float4 vj4 = V0[j];
         const float2 aj = d.aux[j];
         const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-        const float3 e2 = mul3(e, e);
+        // D = (1 + f + dt sum c) I - dt sum cv x x^T: c gets dt tr(Dbar), cv gets -dt x^T Dbar x, x gets
+        // -2 dt cv Dbar x
+        const float3 Dbe = sym_mul(Dbi, Dbi2, e);
         // term owned by i
         {
             const float2 cf = d.cg_coef[at];
@@ -514,10 +534,10 @@ __global__ void __launch_bounds__(kAB) k_adj_visc_coef(Dev d, Params p, const fl
             const float4 xb = px[at];
             PairIn in{e, f3(vi4), f3(vj4), ai.x, aj.x, ai.y, aj.y, vi4.w, vj4.w, xi.w};
             PairBar bar;
-            bar.C = a.x + p.dt * dsumi;
-            bar.Cv = a.y - p.dt * dot3(Dbi, e2);
+            bar.C = a.x + p.dt * tri;
+            bar.Cv = a.y - p.dt * dot3(e, Dbe);
             bar.Bb = f3(bbi);
-            bar.X = f3(xb) + (-2.0f * p.dt * cf.y) * mul3(e, Dbi);
+            bar.X = f3(xb) + (-2.0f * p.dt * cf.y) * Dbe;
             const PairGrad g = pair_reverse(p, in, bar);
             gxi += g.e;
             gvi += g.vo;
@@ -527,22 +547,23 @@ __global__ void __launch_bounds__(kAB) k_adj_visc_coef(Dev d, Params p, const fl
             mu += g.mu;
         }
         // term owned by j (i is its neighbour)
-        {
-            const size_t bt = size_t(rev[at]) * S + j;
+        const unsigned rv = rev[at];
+        if (rv != 255u) {
+            const size_t bt = size_t(rv) * S + j;
             const float2 cf = d.cg_coef[bt];
             const float2 a = pc[bt];
             const float4 xb = px[bt];
-            const float4 Dj = d.jac_d[j];
-            const int mj = int(Dj.w);
-            const float4 Dbj4 = Dbar[j];
-            const float3 Dbj = make_float3(mj & 1 ? 0.f : Dbj4.x, mj & 2 ? 0.f : Dbj4.y, mj & 4 ? 0.f : Dbj4.z);
+            const bool keep_j = d.jac_d2[j].z == 0.0f;
+            const float4 Dbj = keep_j ? Dbar[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 Dbj2 = keep_j ? Dbar2[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float3 ej = (-1.0f) * e;
+            const float3 Dbje = sym_mul(Dbj, Dbj2, ej);
             PairIn in{ej, f3(vj4), f3(vi4), aj.x, ai.x, aj.y, ai.y, vj4.w, vi4.w, xj.w};
             PairBar bar;
             bar.C = a.x + p.dt * (Dbj.x + Dbj.y + Dbj.z);
-            bar.Cv = a.y - p.dt * dot3(Dbj, e2);
+            bar.Cv = a.y - p.dt * dot3(ej, Dbje);
             bar.Bb = f3(bbar[j]);
-            bar.X = f3(xb) + (-2.0f * p.dt * cf.y) * mul3(ej, Dbj);
+            bar.X = f3(xb) + (-2.0f * p.dt * cf.y) * Dbje;
             const PairGrad g = pair_reverse(p, in, bar);
             gxi -= g.e;
             gvi += g.vn;
@@ -682,14 +703,14 @@ __global__ void __launch_bounds__(kAB) k_adj_dens_b(Dev d, Params p, const float
 }
 
 // Per-scene sums of the sigma / mu shares (one block per scene, fixed order: deterministic).
-__global__ void k_adj_param_reduce(Dev d, Params p, const float* gsig, const float* gmu, double* gparam) {
+__global__ void k_adj_param_reduce(Dev d, Params p, const double* gsig, const double* gmu, double* gparam) {
     __shared__ double sa[256], sb[256];
     const int s = blockIdx.x;
     const Scene& sc = d.scenes[s];
     double a = 0.0, b = 0.0;
     for (int i = sc.slot_begin + threadIdx.x; i < sc.slot_begin + sc.n; i += blockDim.x) {
-        a += double(gsig[i]);
-        b += double(gmu[i]);
+        a += gsig[i];
+        b += gmu[i];
     }
     sa[threadIdx.x] = a;
     sb[threadIdx.x] = b;
@@ -733,7 +754,7 @@ size_t store_bytes(const mps_handle* h, int nsteps, int every) {
     size_t b = (ncp + 1 + size_t(every)) * state;
     b += (3 * (K + 1) + 1) * S * sizeof(float4);            // tapes u (DF, CD), q, x
     b += 2 * K * S * (sizeof(float) + 1) + S;               // stiffness, codes, collision codes
-    b += 9 * S * sizeof(float4) + 6 * S * sizeof(float);    // cotangents
+    b += 10 * S * sizeof(float4) + 4 * S * sizeof(float) + 2 * S * sizeof(double);   // cotangents
     b += cap * S * (sizeof(float2) + sizeof(float4) + 1);   // per-pair cotangents + reverse index
     b += size_t(h->nscenes) * 2 * sizeof(double) + 64;
     return b;
@@ -781,12 +802,14 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     ADJ_TRY(alloc(&A.t_cdf, S * K, t));
     ADJ_TRY(alloc(&A.t_ccd, S * K, t));
     ADJ_TRY(alloc(&A.t_adv, S, t));
-    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.gg};
+    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.Dbar2, &A.gg};
     for (float4** q : f4) ADJ_TRY(alloc(q, S, t));
     ADJ_TRY(alloc(&A.gx_id, size_t(std::max<int64_t>(h->n, 1)), t));
     ADJ_TRY(alloc(&A.gv_id, size_t(std::max<int64_t>(h->n, 1)), t));
-    float** f1[] = {&A.grho, &A.galpha, &A.gdelta, &A.gsf, &A.gsig, &A.gmu};
+    float** f1[] = {&A.grho, &A.galpha, &A.gdelta, &A.gsf};
     for (float** q : f1) ADJ_TRY(alloc(q, S, t));
+    ADJ_TRY(alloc(&A.gsig, S, t));
+    ADJ_TRY(alloc(&A.gmu, S, t));
     ADJ_TRY(alloc(&A.pc, S * cap, t));
     ADJ_TRY(alloc(&A.px, S * cap, t));
     ADJ_TRY(alloc(&A.rev, S * cap, t));
@@ -798,6 +821,8 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     // zero what the kernels read before writing (padding slots of the cotangents)
     for (float4** q : f4) ADJ_TRY(cudaMemset(*q, 0, S * sizeof(float4)));
     for (float** q : f1) ADJ_TRY(cudaMemset(*q, 0, S * sizeof(float)));
+    ADJ_TRY(cudaMemset(A.gsig, 0, S * sizeof(double)));
+    ADJ_TRY(cudaMemset(A.gmu, 0, S * sizeof(double)));
     return MPS_OK;
 }
 
@@ -896,17 +921,18 @@ int adjoint_step(mps_handle* h, cudaStream_t s) {
     ADJ_TRY(cudaMemsetAsync(A.px, 0, cap * S * sizeof(float4), s));
     ADJ_TRY(cudaMemsetAsync(A.bbar, 0, S * sizeof(float4), s));
     ADJ_TRY(cudaMemsetAsync(A.Dbar, 0, S * sizeof(float4), s));
+    ADJ_TRY(cudaMemsetAsync(A.Dbar2, 0, S * sizeof(float4), s));
     ADJ_TRY(cudaMemcpyAsync(A.qbar0, A.gv, S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
     float4* qa = A.qbar0;
     float4* qb = A.qbar1;
     for (int k = K - 1; k >= 0; --k) {
         k_adj_jacobi<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.rev, A.t_q + size_t(k) * S, A.t_q + size_t(k + 1) * S, qa, qb,
-                                         A.bbar, A.Dbar, A.pc, A.px);
+                                         A.bbar, A.Dbar, A.Dbar2, A.pc, A.px);
         std::swap(qa, qb);
     }
     const float4* V0 = A.t_udf + size_t(K) * S;   // pre-solve velocity = DF output
-    k_adj_visc_coef<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.rev, qa, A.bbar, A.Dbar, A.pc, A.px, A.gv, A.gx, A.grho,
-                                        A.gsf, A.gsig, A.gmu);
+    k_adj_visc_coef<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.rev, qa, A.bbar, A.Dbar, A.Dbar2, A.pc, A.px, A.gv, A.gx,
+                                        A.grho, A.gsf, A.gsig, A.gmu);
     k_adj_stfac<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.gsf, A.gv, A.gx);
     // divergence-free solve
     for (int k = K - 1; k >= 0; --k) {
@@ -950,6 +976,15 @@ extern "C" {
 int64_t mps_adjoint_memory(mps_handle* h, int32_t nsteps, int32_t every) {
     if (!h || !h->layout_ready || nsteps <= 0 || every <= 0) return -1;
     return int64_t(store_bytes(h, nsteps, every));
+}
+
+int mps_adjoint_reserve(mps_handle* h, int32_t nsteps, int32_t every) {
+    int r = host::check_ready(h);
+    if (r) return r;
+    if ((r = check_adjoint_config(h))) return r;
+    if (nsteps <= 0 || every <= 0) return fail(MPS_E_INVALID, "nsteps and checkpoint_every must be positive");
+    Guard g(h->device);
+    return ensure_store(h, nsteps, every);
 }
 
 int mps_adjoint_forward(mps_handle* h, int32_t nsteps, int32_t every, void* stream) {
@@ -1022,8 +1057,8 @@ int mps_adjoint_backward(mps_handle* h, const float* g_pos4, const float* g_vel4
             if ((r = adjoint_step(h, s))) return r;
             const Dev d = host::make_dev(h, h->cur);
             k_adj_param_reduce<<<h->nscenes, 256, 0, s>>>(d, p, A.gsig, A.gmu, A.gparam);
-            ADJ_TRY(cudaMemsetAsync(A.gsig, 0, S * sizeof(float), s));
-            ADJ_TRY(cudaMemsetAsync(A.gmu, 0, S * sizeof(float), s));
+            ADJ_TRY(cudaMemsetAsync(A.gsig, 0, S * sizeof(double), s));
+            ADJ_TRY(cudaMemsetAsync(A.gmu, 0, S * sizeof(double), s));
             ADJ_TRY(cudaGetLastError());
         }
     }

@@ -174,6 +174,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.cg_b = h->cg_b;
     d.cg_coef = h->cg_coef;
     d.jac_d = h->cg_ap;
+    d.jac_d2 = h->cg_r;
     d.tape_code = nullptr;
     d.tape_adv = nullptr;
     d.bpos = h->bpos;

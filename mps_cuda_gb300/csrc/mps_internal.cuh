@@ -108,7 +108,8 @@ struct Dev {
     float4* color;
     float4 *cg_x, *cg_r, *cg_p, *cg_ap, *cg_b;
     float2* cg_coef;              // per fluid pair, interleaved like nbr_f: (c_ij, cv_ij) of the CG operator
-    float4* jac_d;                // Jacobi: diagonal of A_0 + f I per component (aliases cg_ap)
+    float4* jac_d;                // Jacobi: inverse of the 3x3 diagonal block of A_0 + f I: (xx, yy, zz, xy) (aliases cg_ap)
+    float4* jac_d2;               //   (xz, yz, 1 if the block was replaced by (1 + f) I, 0) (aliases cg_r)
     unsigned char* tape_code;     // adjoint recording (null in plain steps): stiffness branch per slot
     unsigned char* tape_adv;      // adjoint recording: collision branch per slot (2 bits per axis)
     const float4* bpos;           // boundary (x, y, z, h)

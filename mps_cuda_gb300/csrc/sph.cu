@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     const float vs = 10.0f * p.rho0 * p.visc / ai.x;
     const int nf = int(d.cnt[i] & 0xffffu);
     float bx = 0.0f, by = 0.0f, bz = 0.0f;
-    float csum = 0.0f, vx2 = 0.0f, vy2 = 0.0f, vz2 = 0.0f;   // Jacobi diagonal sums
+    float csum = 0.0f, sxx = 0.0f, syy = 0.0f, szz = 0.0f, sxy = 0.0f, sxz = 0.0f, syz = 0.0f;  // Jacobi block sums
     for (int k = 0; k < nf; ++k) {
         const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
         const float4 xj = d.pos[j];
@@ -699,20 +699,29 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
         cf.y = vs * mbar * inv_rj / (d2 + eps_h2) * G / (dist + kFltEps);
         d.cg_coef[size_t(k) * stride + size_t(i)] = cf;
         csum += cf.x;
-        vx2 += cf.y * dx * dx; vy2 += cf.y * dy * dy; vz2 += cf.y * dz * dz;
+        sxx += cf.y * dx * dx; syy += cf.y * dy * dy; szz += cf.y * dz * dz;
+        sxy += cf.y * dx * dy; sxz += cf.y * dx * dz; syz += cf.y * dy * dz;
     }
     d.cg_b[i] = make_float4(vi.x + st_scale * bx, vi.y + st_scale * by, vi.z + st_scale * bz, 0.0f);
     d.cg_x[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
     if (p.visc_solver == 1) {
-        // diag(A_0 + f I) per component; a non-positive entry is replaced by 1 + f and flagged in w
+        // 3x3 diagonal block of A_0 + f I, (1 + f + dt sum c) I - dt sum cv x x^T, inverted by
+        // cofactors; a block with det <= 1e-30 (or not finite) is replaced by (1 + f) I and flagged
         const float f1 = 1.0f + p.cg_factor;
-        float4 D = make_float4(f1 + p.dt * (csum - vx2), f1 + p.dt * (csum - vy2), f1 + p.dt * (csum - vz2), 0.0f);
-        int mask = 0;
-        if (!(D.x > 1.0e-6f)) { D.x = f1; mask |= 1; }
-        if (!(D.y > 1.0e-6f)) { D.y = f1; mask |= 2; }
-        if (!(D.z > 1.0e-6f)) { D.z = f1; mask |= 4; }
-        D.w = float(mask);
-        d.jac_d[i] = D;
+        const float dg = f1 + p.dt * csum;
+        const float axx = dg - p.dt * sxx, ayy = dg - p.dt * syy, azz = dg - p.dt * szz;
+        const float axy = -p.dt * sxy, axz = -p.dt * sxz, ayz = -p.dt * syz;
+        const float c00 = ayy * azz - ayz * ayz, c01 = axz * ayz - axy * azz, c02 = axy * ayz - axz * ayy;
+        const float det = axx * c00 + axy * c01 + axz * c02;
+        if (det > 1.0e-30f && isfinite(det)) {
+            const float id = 1.0f / det;
+            d.jac_d[i] = make_float4(c00 * id, (axx * azz - axz * axz) * id, (axx * ayy - axy * axy) * id, c01 * id);
+            d.jac_d2[i] = make_float4(c02 * id, (axy * axz - axx * ayz) * id, 0.0f, 0.0f);
+        } else {
+            const float id = 1.0f / f1;
+            d.jac_d[i] = make_float4(id, id, id, 0.0f);
+            d.jac_d2[i] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+        }
     }
 }
 
@@ -842,7 +851,8 @@ __global__ void __launch_bounds__(BS) k_cg_dir(Dev d, Params p, unsigned long lo
     d.cg_p[i] = q;
 }
 
-// One Jacobi sweep: r = b + f x0 - (A_0 + f I) q, q' = q + r / D, with r.r of the input iterate
+// One block-Jacobi sweep: r = b + f x0 - (A_0 + f I) q, q' = q + D^-1 r (D: the particle's 3x3
+// diagonal block), with r.r of the input iterate
 // reduced per scene for the stop test (r.r < cg_tol, as the CG's, MPSSolver.cuh:33-41).  The
 // iterates alternate between cg_x (even) and cg_p (odd) by the scene's loop counter, so that one
 // launch per sweep suffices; src/dst given = explicit buffers (adjoint recording).
@@ -865,11 +875,13 @@ __global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long lo
         const float4 b = d.cg_b[i];
         const float4 v0 = d.vel[i];
         const float4 qi = q[i];
-        const float4 D = d.jac_d[i];
+        const float4 m = d.jac_d[i];
+        const float4 m2 = d.jac_d2[i];
         const float f = p.cg_factor;
         const float rx = b.x + f * v0.x - a.x, ry = b.y + f * v0.y - a.y, rz = b.z + f * v0.z - a.z;
         rr = rx * rx + ry * ry + rz * rz;
-        qn[i] = make_float4(qi.x + rx / D.x, qi.y + ry / D.y, qi.z + rz / D.z, 0.0f);
+        qn[i] = make_float4(qi.x + (m.x * rx + m.w * ry + m2.x * rz), qi.y + (m.w * rx + m.y * ry + m2.y * rz),
+                            qi.z + (m2.x * rx + m2.y * ry + m.z * rz), 0.0f);
     }
     const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;

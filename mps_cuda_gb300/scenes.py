@@ -206,11 +206,19 @@ def batched_scenes(nscenes: int = 256, seed: int = 0, nmin: int = 2000, nmax: in
 
 
 def adjoint_16k(seed: int = 0) -> Scene:
+    """32 x 32 x 16 block (r = 0.01) in a unit box, v0 ~ N(0, 0.1) per component, 30 fixed
+    iterations per solve (Jacobi viscosity / surface tension), 200 steps."""
     sc = dam_break((32, 32, 16), 0.02, 0.01, 0.002, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), seed=seed, dt=1.0e-3,
-                   name="adjoint_16k", steps=200, config=dict(fixed_iters=30))
+                   name="adjoint_16k", steps=200, config=dict(fixed_iters=30, visc_solver=L.VISC_JACOBI))
     rng = np.random.default_rng(seed + 17)
     sc.vel4[:, :3] = rng.normal(0.0, 0.1, size=(sc.n, 3)).astype(np.float32)
+    sc.meta["target"] = tuple(float(t) for t in rng.uniform(0.3, 0.7, size=3))
     return sc
+
+
+def adjoint_scenes(nscenes: int = 32, seed: int = 0) -> list[Scene]:
+    """The adjoint benchmark's batch: `nscenes` seeded adjoint_16k scenes, each with its target."""
+    return [adjoint_16k(seed * 1000003 + s) for s in range(nscenes)]
 
 
 def reference_surface_tension(size: int = 5) -> Scene:

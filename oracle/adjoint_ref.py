@@ -2,10 +2,11 @@
 GPU adjoint, never a product path).
 
 A PyTorch float64 CPU restatement of the differentiated step (the adjoint form's forward, fixed
-iteration counts, point-Jacobi viscosity / surface-tension solve): density and alpha, gravity,
-K divergence-free iterations, the viscosity + surface tension + XSPH system by K Jacobi sweeps,
+iteration counts, 3x3 block-Jacobi viscosity / surface-tension solve): density and alpha, gravity,
+K divergence-free iterations, the viscosity + surface tension + XSPH system by K block-Jacobi sweeps,
 K constant-density iterations, box collision and advection.  Neighbour pairs are found by brute
-force from the detached positions with the reference's test |x_i - x_j| < (h_i + h_j) / 2
+force (a k-d tree for large sets) from the detached positions with the reference's test
+|x_i - x_j| < (h_i + h_j) / 2
 (MPSSPHKernel.cuh:17-26), so they are piecewise constant in x exactly as in the GPU adjoint.
 `torch.autograd` of this forward is the FP64 reference gradient; the forward itself is pinned
 against the C++ FP64 oracle (mps_oracle.cpp, visc_solver = 1) at the same settings.
@@ -89,12 +90,34 @@ def pairs(x: torch.Tensor, h: torch.Tensor, y: torch.Tensor | None = None, hy: t
     same = y is None
     y = x if same else y
     hy = h if same else hy
+    if x.shape[0] * y.shape[0] > 2 ** 24:
+        return _pairs_tree(x, h, y, hy, same)
     d = torch.cdist(x, y)
     m = d < 0.5 * (h[:, None] + hy[None, :])
     if same:
         m.fill_diagonal_(False)
     I, J = torch.nonzero(m, as_tuple=True)
     return I, J
+
+
+def _pairs_tree(x, h, y, hy, same):
+    """The same pairs through a k-d tree (large sets): candidates within the largest support, then
+    the exact test."""
+    from scipy.spatial import cKDTree
+    xn, yn = x.numpy(), y.numpy()
+    rmax = float(0.5 * (h.max() + hy.max()))
+    ta = cKDTree(xn)
+    tb = ta if same else cKDTree(yn)
+    coo = ta.sparse_distance_matrix(tb, rmax, output_type="ndarray")
+    I = torch.from_numpy(coo["i"].astype(np.int64))
+    J = torch.from_numpy(coo["j"].astype(np.int64))
+    d = (x[I] - y[J]).norm(dim=1)
+    m = d < 0.5 * (h[I] + hy[J])
+    if same:
+        m &= I != J
+    I, J = I[m], J[m]
+    order = torch.argsort(I * y.shape[0] + J)
+    return I[order], J[order]
 
 
 def boundary_volume(bpos4: np.ndarray, cubic: bool) -> np.ndarray:
@@ -188,15 +211,17 @@ class Rollout:
         cij = st_scale[I] * c + (self.xsph / dt) * (m[J] / rho[J]) * Wf
         cv = 10.0 * rho0 * visc / rho[I] * mbar / rho[J] / (r * r + 0.01 * hI * hI) * Gf / (r + FLT_EPS)
         fct = self.factor
-        D = (1.0 + fct) + dt * (ssum(cij, I)[:, None] - ssum(cv[:, None] * e * e, I))
-        D = torch.where(D > 1.0e-6, D, torch.full_like(D, 1.0 + fct))
+        eye = torch.eye(3, dtype=torch.float64)
+        D = ((1.0 + fct) + dt * ssum(cij, I))[:, None, None] * eye - dt * ssum(cv[:, None, None] * (e[:, :, None] * e[:, None, :]), I)
+        ok = (torch.linalg.det(D) > 1.0e-30)[:, None, None]
+        Dinv = torch.where(ok, torch.linalg.inv(torch.where(ok, D, eye)), eye / (1.0 + fct))
         x0 = v
         q = v
         for _ in range(K):
             p = q[I] - q[J]
             acc = ssum(cij[:, None] * p - (cv * (p * e).sum(1))[:, None] * e, I)
             Aq = q * (1.0 + fct) + dt * acc
-            q = q + (b + fct * x0 - Aq) / D
+            q = q + (Dinv @ (b + fct * x0 - Aq)[:, :, None])[:, :, 0]
         v = q
 
         v = pressure(v, False)

@@ -538,10 +538,33 @@ double dot3n(const std::vector<d3>& a, const std::vector<d3>& b) {
     return s;
 }
 
-// Diagonal of A_0 + f I per component: (1 + f) + dt [sum_j (ST + XSPH coefficient) -
-// sum_j (viscosity coefficient) x_ij,c^2], the coefficients of cg_apply's terms; a non-positive
-// entry is replaced by 1 + f.
-void jacobi_diag(const orc_sim& s, std::vector<d3>& D, double factor) {
+// 3x3 diagonal block of A_0 + f I per particle (symmetric):
+// (1 + f) I + dt [sum_j (ST + XSPH coefficient) I - sum_j (viscosity coefficient) x_ij x_ij^T],
+// the coefficients of cg_apply's terms; returned inverted (6 entries xx, yy, zz, xy, xz, yz).
+// A block with a non-positive or non-finite determinant is replaced by (1 + f) I.
+struct Sym3 {
+    double xx, yy, zz, xy, xz, yz;
+};
+Sym3 sym3_inverse(const Sym3& a, double fallback, bool* ok) {
+    const double c00 = a.yy * a.zz - a.yz * a.yz;
+    const double c01 = a.xz * a.yz - a.xy * a.zz;
+    const double c02 = a.xy * a.yz - a.xz * a.yy;
+    const double det = a.xx * c00 + a.xy * c01 + a.xz * c02;
+    if (!(det > 1.0e-30) || !std::isfinite(det)) {
+        *ok = false;
+        return Sym3{1.0 / fallback, 1.0 / fallback, 1.0 / fallback, 0.0, 0.0, 0.0};
+    }
+    *ok = true;
+    const double id = 1.0 / det;
+    return Sym3{c00 * id, (a.xx * a.zz - a.xz * a.xz) * id, (a.xx * a.yy - a.xy * a.xy) * id, c01 * id, c02 * id,
+                (a.xy * a.xz - a.xx * a.yz) * id};
+}
+inline d3 sym3_mul(const Sym3& m, d3 v) {
+    return d3{m.xx * v.x + m.xy * v.y + m.xz * v.z, m.xy * v.x + m.yy * v.y + m.yz * v.z,
+              m.xz * v.x + m.yz * v.y + m.zz * v.z};
+}
+
+void jacobi_blocks(const orc_sim& s, std::vector<Sym3>& Dinv, double factor) {
     const int64_t n = s.n;
     const double dt = s.p.dt;
 #pragma omp parallel for schedule(static)
@@ -551,7 +574,7 @@ void jacobi_diag(const orc_sim& s, std::vector<d3>& D, double factor) {
         const d3 xi = s.pos[size_t(i)];
         const double mi = s.mass[size_t(i)], di = s.density[size_t(i)];
         double cst = 0.0, cx = 0.0;
-        d3 cv{0, 0, 0};
+        Sym3 cv{0, 0, 0, 0, 0, 0};
         for_nei(s.ff, i, [&](uint32_t jd) {
             const d3 xij = xi - s.pos[jd];
             const double dist = length(xij);
@@ -560,27 +583,30 @@ void jacobi_diag(const orc_sim& s, std::vector<d3>& D, double factor) {
             cx += (s.mass[jd] / s.density[jd]) * WKernel(dist, invHi, s.p.cubic);
             const double c = 0.5 * (mi + s.mass[jd]) / s.density[jd] / (dist * dist + 0.01 * hi * hi) *
                              GKernel(dist, invHi, s.p.cubic) / (dist + kFltEps);
-            cv += d3{c * xij.x * xij.x, c * xij.y * xij.y, c * xij.z * xij.z};
+            cv.xx += c * xij.x * xij.x; cv.yy += c * xij.y * xij.y; cv.zz += c * xij.z * xij.z;
+            cv.xy += c * xij.x * xij.y; cv.xz += c * xij.x * xij.z; cv.yz += c * xij.y * xij.z;
         });
         const double c0 = (dt * s.p.surface_tension / mi) * cst + (s.p.xsph / dt) * cx;
         const double vs = 10.0 * s.p.mat_density * s.p.viscosity / di;
-        auto diag = [&](double cvc) {
-            const double v = (1.0 + factor) + dt * (c0 - vs * cvc);
-            return v > 1.0e-6 ? v : 1.0 + factor;
-        };
-        D[size_t(i)] = d3{diag(cv.x), diag(cv.y), diag(cv.z)};
+        const double dg = (1.0 + factor) + dt * c0;
+        const Sym3 D{dg - dt * vs * cv.xx, dg - dt * vs * cv.yy, dg - dt * vs * cv.zz, -dt * vs * cv.xy,
+                     -dt * vs * cv.xz, -dt * vs * cv.yz};
+        bool ok;
+        Dinv[size_t(i)] = sym3_inverse(D, 1.0 + factor, &ok);
     }
 }
 
-// Point-Jacobi alternative of the CG on the same system: from x0 = v,
-// x += D^-1 (b + f x0 - (A_0 + f I) x) until r.r < cg_tol (at most cg_max_iter sweeps) or for
-// fixed_iters sweeps (the reference's legacy Jacobi viscosity, MPSSPHNonPressureUtil.cuh:90-195,
-// iterated a block-diagonal inverse on the viscosity term alone).
+// Block-Jacobi alternative of the CG on the same system: from x0 = v,
+// x += D^-1 (b + f x0 - (A_0 + f I) x), D = the 3x3 diagonal blocks, until r.r < cg_tol (at most
+// cg_max_iter sweeps) or for fixed_iters sweeps (the reference's legacy Jacobi viscosity,
+// MPSSPHNonPressureUtil.cuh:90-195, also inverted each particle's 3x3 block, there of the
+// viscosity term alone).
 int viscst_jacobi(orc_sim& s, double* rr_out) {
     const int64_t n = s.n;
     const double f = 0.01;   // the CG iterations' operator factor (MPSSPHNonPressureUtil.cu:165-169)
-    std::vector<d3> D(static_cast<size_t>(n)), Ax(static_cast<size_t>(n));
-    jacobi_diag(s, D, f);
+    std::vector<Sym3> Dinv(static_cast<size_t>(n));
+    std::vector<d3> Ax(static_cast<size_t>(n));
+    jacobi_blocks(s, Dinv, f);
     std::vector<d3>& x = s.predict;
     const std::vector<d3> x0 = s.vel;
     int l = 1;
@@ -597,10 +623,7 @@ int viscst_jacobi(orc_sim& s, double* rr_out) {
         }
         *rr_out = rr;
         if (s.p.fixed_iters <= 0 && rr < s.p.cg_tol) break;
-        for (int64_t i = 0; i < n; ++i) {
-            const d3 d = D[size_t(i)];
-            x[size_t(i)] += d3{r[size_t(i)].x / d.x, r[size_t(i)].y / d.y, r[size_t(i)].z / d.z};
-        }
+        for (int64_t i = 0; i < n; ++i) x[size_t(i)] += sym3_mul(Dinv[size_t(i)], r[size_t(i)]);
         l++;
     }
     return l;

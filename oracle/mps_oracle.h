@@ -58,7 +58,7 @@ typedef struct orc_params {
     int32_t zsort;             /* 1: Morton re-sort when frame % 50 == 1 (MPSSystem.cpp:220-224) */
     int32_t threads;           /* OpenMP threads, 0 = default */
     int32_t fixed_iters;       /* > 0: DF, CD and CG run exactly this many iterations (no early exit) */
-    int32_t visc_solver;       /* 0 CG (the reference's), 1 point-Jacobi sweeps on the same system */
+    int32_t visc_solver;       /* 0 CG (the reference's), 1 block-Jacobi sweeps on the same system */
 } orc_params;
 
 typedef struct orc_stats {
