@@ -163,7 +163,8 @@ def run_ours(args, scene, rank, world, local_rank):
     runs = [st1["runs_total"][k] - st0["runs_total"][k] for k in range(3)]
     iters = [st1["iters_total"][k] - st0["iters_total"][k] for k in range(3)]
     P = radix_passes(sim)
-    launches = sum(sim.launches_per_step((0, 0, 0), P) for _ in range(args.steps)) + 2 * runs[0] + 3 * runs[1] + 2 * runs[2]
+    static = sim.launches_per_step((0, 0, 0), P)
+    launches = args.steps * static + sim.launches_per_step(tuple(runs), P) - static
 
     # ---- e2e through the host-buffer C-ABI call (pinned H2D + step + D2H every step), replaying
     # the timed steps from the same starting state

@@ -79,7 +79,7 @@ void mps_handle::release() {
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
                      (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&nbr_l, (void**)&stage, (void**)&rho,
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
-                     (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_coef,
+                     (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol,
                      (void**)&partial, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
                      (void**)&keys, (void**)&keys_tmp, (void**)&vals, (void**)&vals_tmp, (void**)&sort_counts,
@@ -172,6 +172,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.cg_p = h->cg_p;
     d.cg_ap = h->cg_ap;
     d.cg_b = h->cg_b;
+    d.cg_s = h->cg_s;
     d.cg_coef = h->cg_coef;
     d.jac_d = h->cg_ap;
     d.jac_d2 = h->cg_r;
@@ -290,7 +291,7 @@ int allocate(mps_handle* h) {
     for (float* z : zf) MPS_CUDA_TRY(cudaMemset(z, 0, S * sizeof(float)));
     MPS_CUDA_TRY(cudaMemset(h->aux, 0, S * sizeof(float2)));
     MPS_CUDA_TRY(cudaMemset(h->color, 0, S * sizeof(float4)));
-    float4** cgv[] = {&h->cg_x, &h->cg_r, &h->cg_p, &h->cg_ap, &h->cg_b};
+    float4** cgv[] = {&h->cg_x, &h->cg_r, &h->cg_p, &h->cg_ap, &h->cg_b, &h->cg_s};
     for (float4** v : cgv) {
         MPS_CUDA_TRY(dalloc(v, S));
         MPS_CUDA_TRY(cudaMemset(*v, 0, S * sizeof(float4)));
@@ -393,8 +394,7 @@ int eager_loop(mps_handle* h, cudaStream_t s, int kind /*0 DF,1 CG,2 CD*/) {
             launch_jacobi(d, p, bs, 0ull, 0, 0, nullptr, nullptr, s);
         } else if (kind == 1) {
             launch_cg_ap(d, p, bs, 0ull, 0, s);
-            launch_cg_update(d, p, bs, s);
-            launch_cg_dir(d, p, bs, 0ull, 0, 0, s);
+            launch_cg_update(d, p, bs, 0ull, 0, 0, s);
         } else {
             launch_pressure_A(d, p, kind == 0 ? 0 : 1, bs, 0ull, 0, s);
             launch_pressure_B(d, p, bs, 0ull, 0, 0, s);
@@ -561,8 +561,7 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
                 launch_jacobi(d, p, bs, hcg, 1, loop_limit(h, 1), nullptr, nullptr, b.s);
             } else {
                 launch_cg_ap(d, p, bs, hcg, 1, b.s);
-                launch_cg_update(d, p, bs, b.s);
-                launch_cg_dir(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+                launch_cg_update(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
             }
             MPS_CAP_TRY(cudaGetLastError());
             MPS_CAP_TRY(seg_end(b));

@@ -51,7 +51,7 @@ struct mps_handle {
     float *rho = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
     float2* aux = nullptr;
     float4* color = nullptr;
-    float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr;
+    float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr, *cg_s = nullptr;
     float2* cg_coef = nullptr;
     float4* bpos = nullptr;
     float* bvol = nullptr;

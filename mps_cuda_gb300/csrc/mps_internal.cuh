@@ -50,9 +50,9 @@ struct SceneSolve {
     int iter;         // reference loop counter l
     int blocks_done;  // blocks of this scene finished in the current pass
     double err;       // last mean error (pressure) or r.r (CG)
-    double rr;        // CG: r.r of this iteration
-    double cg_alpha;  // CG step length
-    double cg_beta;   // CG direction update
+    double rr;        // CG: r.r of the last operator pass
+    double cg_alpha;  // CG step length of the last iteration
+    double cg_beta;   // CG direction coefficient of the last iteration
 };
 
 struct StepCounters {
@@ -107,6 +107,7 @@ struct Dev {
     float2* aux;                  // (rho, st factor) packed for the CG gathers
     float4* color;
     float4 *cg_x, *cg_r, *cg_p, *cg_ap, *cg_b;
+    float4* cg_s;                 // CG: s = A p kept by recurrence
     float2* cg_coef;              // per fluid pair, interleaved like nbr_f: (c_ij, cv_ij) of the CG operator
     float4* jac_d;                // Jacobi: inverse of the 3x3 diagonal block of A_0 + f I: (xx, yy, zz, xy) (aliases cg_ap)
     float4* jac_d2;               //   (xz, yz, 1 if the block was replaced by (1 + f) I, 0) (aliases cg_r)
@@ -198,6 +199,54 @@ struct Kahan {
     }
 };
 
+// Neighbour loops are latency-bound (a dependent index load, then gathers).  visit_batched walks
+// the interleaved list of slot i (item k at list[k * stride + i]) in batches of B: phase 1 loads
+// the batch's indices and the per-pair data streamed in the same layout (stream(k)), phase 2
+// issues every gather (gather(j, k)), phase 3 runs use(gathered, streamed, k) in k order.  A
+// thread so keeps B index + stream loads, then B gathers, in flight, and sums in the same order as
+// a plain loop (results are bit-identical for every B).
+struct NoStream {};
+template <int B, class S, class T, class Stream, class Gather, class Use>
+__device__ __forceinline__ void visit_batched(const unsigned* __restrict__ list, size_t stride, int i, int n,
+                                              Stream stream, Gather gather, Use use) {
+    int k = 0;
+    for (; k + B <= n; k += B) {
+        unsigned jj[B];
+        S ss[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            jj[u] = list[size_t(k + u) * stride + size_t(i)];
+            ss[u] = stream(k + u);
+        }
+        T v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) v[u] = gather(jj[u], k + u);
+#pragma unroll
+        for (int u = 0; u < B; ++u) use(v[u], ss[u], k + u);
+    }
+    for (; k < n; ++k) {
+        const S sk = stream(k);
+        use(gather(list[size_t(k) * stride + size_t(i)], k), sk, k);
+    }
+}
+
+// Batch sizes per loop (template arguments of visit_batched), set from GB300 sweeps.
+#ifndef MPSG_B_AP
+#define MPSG_B_AP 4      // CG / Jacobi operator
+#endif
+#ifndef MPSG_B_PA
+#define MPSG_B_PA 2      // density change rate (pressure pass A)
+#endif
+#ifndef MPSG_B_PB
+#define MPSG_B_PB 4      // pressure force (pass B)
+#endif
+#ifndef MPSG_B_DENS
+#define MPSG_B_DENS 2    // density and alpha
+#endif
+#ifndef MPSG_B_SETUP
+#define MPSG_B_SETUP 2   // surface-tension factor and the solve's coefficients (once per step)
+#endif
+
 __device__ __forceinline__ int cell_coord(float x, float o, float inv, int dim) {
     const float t = __fmul_rn(__fsub_rn(x, o), inv);
     if (!(t >= 0.0f)) return 0;
@@ -236,9 +285,8 @@ void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s);
 void launch_cg_ax0(const Dev& d, const Params& p, int bs, cudaStream_t s);
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond,
                   cudaStream_t s);
-void launch_cg_update(const Dev& d, const Params& p, int bs, cudaStream_t s);
-void launch_cg_dir(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
-                   cudaStream_t s);
+void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                      cudaStream_t s);
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);
 // Jacobi sweep of the viscosity/surface-tension system; src/dst null = the two iterate buffers
 // chosen by the scene's loop counter (graph form), else explicit (adjoint recording).

@@ -23,6 +23,11 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// gathered neighbour records of the batched loops
+struct XV { float4 x, v; };
+struct XVA { float4 x, v; float2 a; };
+struct XQ { float4 x, q; };
+
 __device__ __forceinline__ int block_scene(const Dev& d, int bs) {
     return d.chunk_scene[(blockIdx.x * bs) / kChunk];
 }
@@ -372,9 +377,8 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     Kahan rf, gx, gy, gz, sq;
     rf.add(p.V * kW(0.0f, invh, p.cubic));
-    for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
-        const float4 xj = d.pos[j];
+    visit_batched<MPSG_B_DENS, NoStream, float4>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; }, [&](unsigned j, int) { return d.pos[j]; },
+                          [&](const float4& xj, NoStream, int) {
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         const float d2 = dx * dx + dy * dy + dz * dz;
         const float invd = safe_rsqrt(d2);
@@ -384,12 +388,12 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
         const float ax = g * dx, ay = g * dy, az = g * dz;
         gx.add(ax); gy.add(ay); gz.add(az);
         sq.add(ax * ax + ay * ay + az * az);
-    }
+    });
     Kahan rb;
-    for (int k = 0; k < nb; ++k) {
-        const unsigned j = d.nbr_b[size_t(k) * stride + size_t(i)];
-        const float4 xj = d.bpos[j];
-        const float vb = d.bvol[j];
+    visit_batched<MPSG_B_DENS, NoStream, float4>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+                          [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
+                          [&](const float4& xj, NoStream, int) {
+        const float vb = xj.w;
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         const float d2 = dx * dx + dy * dy + dz * dz;
         const float invd = safe_rsqrt(d2);
@@ -397,7 +401,7 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
         rb.add(vb * kW(dist, invh, p.cubic));
         const float g = vb * kG(dist, invd, invh, p.cubic);
         gx.add(g * dx); gy.add(g * dy); gz.add(g * dz);
-    }
+    });
     const float rho = (rf.s + rb.s) * p.rho0;
     d.rho[i] = rho;
     // alpha denominator in FP64: |sum grad|^2 + sum |grad|^2, clamp at 1e-20 (MPSSPHDFSPHUtil.cuh:127-137)
@@ -465,26 +469,26 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         const unsigned c = d.cnt[i];
         const int nf = int(c & 0xffffu), nb = int(c >> 16);
         float df = 0.0f;
-        for (int k = 0; k < nf; ++k) {
-            const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
-            const float4 xj = d.pos[j];
-            const float4 vj = d.vel[j];
+        visit_batched<MPSG_B_PA, NoStream, XV>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+                          [&](unsigned j, int) { return XV{d.pos[j], d.vel[j]}; },
+                          [&](const XV& t, NoStream, int) {
+            const float4 xj = t.x, vj = t.v;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             const float invd = safe_rsqrt(d2);
             const float g = kG(d2 * invd, invd, invh, p.cubic);
             df += g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
-        }
+        });
         float db = 0.0f;
-        for (int k = 0; k < nb; ++k) {
-            const unsigned j = d.nbr_b[size_t(k) * stride + size_t(i)];
-            const float4 xj = d.bpos[j];
+        visit_batched<MPSG_B_PA, NoStream, float4>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+                              [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
+                              [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             const float invd = safe_rsqrt(d2);
             const float g = kG(d2 * invd, invd, invh, p.cubic);
-            db += d.bvol[j] * g * (dx * vi.x + dy * vi.y + dz * vi.z);
-        }
+            db += xj.w * g * (dx * vi.x + dy * vi.y + dz * vi.z);
+        });
         const float delta = p.V * df + db;
         const float r = d.rho[i] * p.inv_rho0;
         const float ka = delta * p.dt;
@@ -571,29 +575,28 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
             fx -= g * dx; fy -= g * dy; fz -= g * dz;
         }
     } else {
-        for (int k = 0; k < nf; ++k) {
-            const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
-            const float4 xj = d.pos[j];
-            const float kj = d.kappa[j];
+        visit_batched<MPSG_B_PB, NoStream, float4>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+                              [&](unsigned j, int) { float4 x = d.pos[j]; x.w = d.kappa[j]; return x; },
+                              [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             const float invd = safe_rsqrt(d2);
-            const float g = (ki + kj) * kG(d2 * invd, invd, invh, p.cubic);
+            const float g = (ki + xj.w) * kG(d2 * invd, invd, invh, p.cubic);
             fx -= g * dx; fy -= g * dy; fz -= g * dz;
-        }
+        });
     }
     fx *= 0.5f * p.V; fy *= 0.5f * p.V; fz *= 0.5f * p.V;
     if (ki != 0.0f) {
         float bx = 0.0f, by = 0.0f, bz = 0.0f;
-        for (int k = 0; k < nb; ++k) {
-            const unsigned j = d.nbr_b[size_t(k) * stride + size_t(i)];
-            const float4 xj = d.bpos[j];
+        visit_batched<MPSG_B_PB, NoStream, float4>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+                              [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
+                              [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             const float invd = safe_rsqrt(d2);
-            const float g = d.bvol[j] * kG(d2 * invd, invd, invh, p.cubic);
+            const float g = xj.w * kG(d2 * invd, invd, invh, p.cubic);
             bx -= g * dx; by -= g * dy; bz -= g * dz;
-        }
+        });
         const float h = 0.5f * ki;
         fx += h * bx; fy += h * by; fz += h * bz;
     }
@@ -638,16 +641,16 @@ __global__ void __launch_bounds__(BS) k_st_factor(Dev d, Params p) {
     const float invh = 1.0f / xi.w;
     const int nf = int(d.cnt[i] & 0xffffu);
     float acc = 0.0f;
-    for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
-        const float4 xj = d.pos[j];
-        const float4 vj = d.vel[j];
+    visit_batched<MPSG_B_SETUP, NoStream, XV>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+                      [&](unsigned j, int) { return XV{d.pos[j], d.vel[j]}; },
+                      [&](const XV& t, NoStream, int) {
+        const float4 xj = t.x, vj = t.v;
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         const float d2 = dx * dx + dy * dy + dz * dz;
         const float invd = safe_rsqrt(d2);
         const float g = kG(d2 * invd, invd, invh, p.cubic);
         acc += vj.w * g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
-    }
+    });
     d.aux[i] = make_float2(d.rho[i], acc);
 }
 
@@ -674,11 +677,11 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     const int nf = int(d.cnt[i] & 0xffffu);
     float bx = 0.0f, by = 0.0f, bz = 0.0f;
     float csum = 0.0f, sxx = 0.0f, syy = 0.0f, szz = 0.0f, sxy = 0.0f, sxz = 0.0f, syz = 0.0f;  // Jacobi block sums
-    for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * stride + size_t(i)];
-        const float4 xj = d.pos[j];
-        const float4 vj = d.vel[j];
-        const float2 aj = d.aux[j];
+    visit_batched<MPSG_B_SETUP, NoStream, XVA>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+                       [&](unsigned j, int) { return XVA{d.pos[j], d.vel[j], d.aux[j]}; },
+                       [&](const XVA& t, NoStream, int k) {
+        const float4 xj = t.x, vj = t.v;
+        const float2 aj = t.a;
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         const float d2 = dx * dx + dy * dy + dz * dz;
         const float invd = safe_rsqrt(d2);
@@ -701,7 +704,7 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
         csum += cf.x;
         sxx += cf.y * dx * dx; syy += cf.y * dy * dy; szz += cf.y * dz * dz;
         sxy += cf.y * dx * dy; sxz += cf.y * dx * dz; syz += cf.y * dy * dz;
-    }
+    });
     d.cg_b[i] = make_float4(vi.x + st_scale * bx, vi.y + st_scale * by, vi.z + st_scale * bz, 0.0f);
     d.cg_x[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
     if (p.visc_solver == 1) {
@@ -733,24 +736,29 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
     const float4 qi = q[i];
     const int nf = int(d.cnt[i] & 0xffffu);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for (int k = 0; k < nf; ++k) {
-        const size_t at = size_t(k) * stride + size_t(i);
-        const unsigned j = d.nbr_f[at];
-        const float2 cf = d.cg_coef[at];
-        const float4 xj = d.pos[j];
-        const float4 qj = q[j];
+    visit_batched<MPSG_B_AP, float2, XQ>(d.nbr_f, stride, i, nf,
+                       [&](int k) { return d.cg_coef[size_t(k) * stride + size_t(i)]; },
+                       [&](unsigned j, int) { return XQ{d.pos[j], q[j]}; },
+                       [&](const XQ& g, const float2& cf, int) {
+        const float4 xj = g.x, qj = g.q;
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         const float px = qi.x - qj.x, py = qi.y - qj.y, pz = qi.z - qj.z;
         const float t = cf.y * (px * dx + py * dy + pz * dz);
         sx += cf.x * px - t * dx;
         sy += cf.x * py - t * dy;
         sz += cf.x * pz - t * dz;
-    }
+    });
     const float f1 = 1.0f + factor;
     return make_float3(qi.x * f1 + p.dt * sx, qi.y * f1 + p.dt * sy, qi.z * f1 + p.dt * sz);
 }
 
-// A x0 with factor 0; r = b - A x0; p = r (MPSSolver.cuh:24-28).
+// A x0 with factor 0; r = b - A x0 (MPSSolver.cuh:24-28).  The CG below runs in the
+// Chronopoulos-Gear arrangement (the same iterates as the reference's CGSolver in exact
+// arithmetic): per iteration one operator pass w = A r with the dots r.r and r.w, then one vector
+// pass p = r + beta p, s = w + beta s (s = A p), x += alpha p, r -= alpha s, where
+// beta = (r.r) / (r.r)_old and alpha = (r.r) / (r.w - beta (r.r) / alpha_old) (first iteration:
+// beta = 0, alpha = (r.r) / (r.w)).  The stop test r.r < tol and the loop counter are the
+// reference's (MPSSolver.cuh:33-60).  p and s start at zero.
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
@@ -758,12 +766,13 @@ __global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
     if (i >= sc.slot_begin + sc.n) return;
     const float3 a = apply_A(d, p, i, d.cg_x, 0.0f);
     const float4 b = d.cg_b[i];
-    const float4 r = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
-    d.cg_r[i] = r;
-    d.cg_p[i] = r;
+    d.cg_r[i] = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
+    d.cg_p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    d.cg_s[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// A p, dots r.r and p.Ap in FP64, convergence decision and step length (MPSSolver.cuh:33-49).
+// w = A r, dots r.r and r.w (FP32 per thread, FP64 across warps and blocks), the stop test and
+// the step coefficients (MPSSolver.cuh:33-49 in the Chronopoulos-Gear arrangement).
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long long cond, int use_cond) {
     __shared__ double sh[32];
@@ -772,83 +781,66 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
-    float rr = 0.0f, pap = 0.0f;
+    float rr = 0.0f, rw = 0.0f;
     if (i < sc.slot_begin + sc.n) {
-        const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor);
-        d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
+        const float3 w = apply_A(d, p, i, d.cg_r, p.cg_factor);
+        d.cg_ap[i] = make_float4(w.x, w.y, w.z, 0.0f);
         const float4 r = d.cg_r[i];
-        const float4 q = d.cg_p[i];
         rr = r.x * r.x + r.y * r.y + r.z * r.z;
-        pap = q.x * a.x + q.y * a.y + q.z * a.z;
+        rw = r.x * w.x + r.y * w.y + r.z * w.z;
     }
-    const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
+    const double2 bs2 = block_sum2_f<BS>(rr, rw, sh2);
     if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
     const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
-    const double tpap = scene_partial_sum<BS>(d, sc, 1, sh);
+    const double trw = scene_partial_sum<BS>(d, sc, 1, sh);
     if (threadIdx.x == 0) {
         SceneSolve& S = d.solve[s];
         const int l = S.iter;
         const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
         const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
         S.err = trr;
-        S.rr = trr;
         if (stop) {
             S.active = 0;
             S.do_update = 0;
         } else {
+            const double beta = l == 1 ? 0.0 : trr / S.rr;
+            const double denom = l == 1 ? trw : trw - beta * trr / S.cg_alpha;
+            S.cg_beta = beta;
+            S.cg_alpha = trr / denom;
             S.do_update = 1;
-            S.cg_alpha = trr / tpap;
             S.iter = l + 1;
             if (l + 1 > cap) S.active = 0;
         }
+        S.rr = trr;
         finish_scene_decision(d, p, cond, use_cond);
     }
 }
 
-// x += alpha p; r -= alpha Ap; beta = (r.r)_new / (r.r)_old (MPSSolver.cuh:49-60).
+// p = r + beta p, s = w + beta s, x += alpha p, r -= alpha s (MPSSolver.cuh:49-60,
+// MPSCGKernel.cuh:196-207), in one pass with no reduction; the loop guard of the WHILE body.
 template <int BS>
-__global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p) {
-    __shared__ double sh[32];
-    __shared__ double2 sh2[BS / 32];
-    const int s = block_scene(d, BS);
-    if (!d.solve[s].do_update) return;
-    const Scene& sc = d.scenes[s];
-    const int i = blockIdx.x * BS + threadIdx.x;
-    float rr = 0.0f;
-    if (i < sc.slot_begin + sc.n) {
-        const float a = float(d.solve[s].cg_alpha);
-        float4 x = d.cg_x[i];
-        float4 r = d.cg_r[i];
-        const float4 q = d.cg_p[i];
-        const float4 ap = d.cg_ap[i];
-        x.x += a * q.x; x.y += a * q.y; x.z += a * q.z;
-        r.x -= a * ap.x; r.y -= a * ap.y; r.z -= a * ap.z;
-        d.cg_x[i] = x;
-        d.cg_r[i] = r;
-        rr = r.x * r.x + r.y * r.y + r.z * r.z;
-    }
-    const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
-    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
-    if (!last_block_of_scene<BS>(d, s, sc)) return;
-    const double t = scene_partial_sum<BS>(d, sc, 0, sh);
-    if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
-}
-
-// p = r + beta p (MPSCGKernel.cuh:196-207).
-template <int BS>
-__global__ void __launch_bounds__(BS) k_cg_dir(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+__global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
     const int s = block_scene(d, BS);
     if (!d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
     if (i >= sc.slot_begin + sc.n) return;
+    const float a = float(d.solve[s].cg_alpha);
     const float b = float(d.solve[s].cg_beta);
     const float4 r = d.cg_r[i];
+    const float4 w = d.cg_ap[i];
     float4 q = d.cg_p[i];
+    float4 sv = d.cg_s[i];
+    float4 x = d.cg_x[i];
     q.x = r.x + b * q.x; q.y = r.y + b * q.y; q.z = r.z + b * q.z;
+    sv.x = w.x + b * sv.x; sv.y = w.y + b * sv.y; sv.z = w.z + b * sv.z;
+    x.x += a * q.x; x.y += a * q.y; x.z += a * q.z;
     d.cg_p[i] = q;
+    d.cg_s[i] = sv;
+    d.cg_x[i] = x;
+    d.cg_r[i] = make_float4(r.x - a * sv.x, r.y - a * sv.y, r.z - a * sv.z, 0.0f);
 }
 
 // One block-Jacobi sweep: r = b + f x0 - (A_0 + f I) q, q' = q + D^-1 r (D: the particle's 3x3
@@ -1057,12 +1049,9 @@ void launch_cg_ax0(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
 }
-void launch_cg_update(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_update, d, p);
-}
-void launch_cg_dir(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
-                   cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_dir, d, p, cond, use_cond, limit);
+void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                      cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_update, d, p, cond, use_cond, limit);
 }
 void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    const float4* src, float4* dst, cudaStream_t s) {
