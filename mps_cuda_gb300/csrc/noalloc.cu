@@ -28,10 +28,10 @@ namespace {
 constexpr int kMax = MPS_NOALLOC_MAX_PARTICLES;
 constexpr size_t kKeysBytes = size_t(kMax) * sizeof(unsigned long long);
 constexpr size_t kValsBytes = size_t(kMax) * sizeof(unsigned int);
-constexpr size_t kCountsBytes = size_t(256) * ((kMax + 4095) / 4096) * sizeof(unsigned int);
+constexpr size_t kCountsBytes = size_t(256) * ((kMax + 4095) / 4096 + 1) * sizeof(unsigned int);  // + digit totals
 constexpr size_t kScratchBytes = kKeysBytes + kValsBytes + kCountsBytes;
 
-// Scratch of mps_cell_sort_noalloc: [tmp keys | tmp vals | digit histograms].  In host code the
+// Scratch of mps_cell_sort_noalloc: [tmp keys | tmp vals | digit histograms + totals].  In host code the
 // name is only a stand-in; the device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 

@@ -4,7 +4,8 @@
 //
 // One pass per digit (digit_bits <= 8):
 //   upsweep  : per-tile digit histogram (warp-aggregated shared atomics), digit-major counts
-//   scan     : exclusive scan of the digit-major counts (one block)
+//   scan     : per digit, a warp scans that digit's row of tile counts (coalesced, all digits in
+//              parallel); one block scans the 256 digit totals; the downsweep adds both
 //   downsweep: per-warp stable ranks with __match_any_sync, cross-warp prefix per digit, scatter
 // Tiles are 8 warps x 32 lanes x 16 items; each warp owns a contiguous run of 512 keys, so
 // (warp, round, lane) order equals input order and the scatter is stable.
@@ -18,7 +19,6 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kIpt = 16;
 constexpr int kTile = kThreads * kIpt;
 constexpr int kBins = 256;
-constexpr int kScanThreads = 1024;
 
 __global__ void __launch_bounds__(kThreads) rs_upsweep(const unsigned long long* __restrict__ keys, int n,
                                                        int shift, unsigned int mask, int nblocks,
@@ -40,40 +40,45 @@ __global__ void __launch_bounds__(kThreads) rs_upsweep(const unsigned long long*
     counts[threadIdx.x * nblocks + blockIdx.x] = hist[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(kScanThreads) rs_scan(unsigned int* __restrict__ counts, int total) {
-    __shared__ unsigned int warp_sums[kScanThreads / 32];
-    const int chunk = (total + kScanThreads - 1) / kScanThreads;
-    const int begin = threadIdx.x * chunk;
-    const int end = min(begin + chunk, total);
-    unsigned int sum = 0;
-    for (int i = begin; i < end; ++i) sum += counts[i];
-    // block exclusive scan of per-thread sums
+// counts[d * nblocks + b] <- exclusive prefix over tiles b of digit d; totals[d] <- digit total.
+__global__ void __launch_bounds__(kThreads) rs_scan_rows(unsigned int* __restrict__ counts, int nblocks,
+                                                         unsigned int* __restrict__ totals) {
+    const int lane = threadIdx.x & 31;
+    const int digit = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    if (digit >= kBins) return;
+    unsigned int* row = counts + size_t(digit) * size_t(nblocks);
+    unsigned int run = 0;
+    for (int base = 0; base < nblocks; base += 32) {
+        const int idx = base + lane;
+        const unsigned int v = idx < nblocks ? row[idx] : 0u;
+        unsigned int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (idx < nblocks) row[idx] = run + incl - v;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) totals[digit] = run;
+}
+
+// totals[d] <- exclusive prefix over digits (one block of kBins threads).
+__global__ void __launch_bounds__(kBins) rs_scan_digits(unsigned int* __restrict__ totals) {
+    __shared__ unsigned int warp_sums[kBins / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned int incl = sum;
+    const unsigned int v = totals[threadIdx.x];
+    unsigned int incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const unsigned int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
+        const unsigned int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
     }
     if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
-    if (warp == 0) {
-        unsigned int w = warp_sums[lane];
-        unsigned int wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned int v = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += v;
-        }
-        warp_sums[lane] = wi - w;
-    }
-    __syncthreads();
-    unsigned int run = warp_sums[warp] + incl - sum;
-    for (int i = begin; i < end; ++i) {
-        const unsigned int c = counts[i];
-        counts[i] = run;
-        run += c;
-    }
+    unsigned int before = 0;
+    for (int w = 0; w < warp; ++w) before += warp_sums[w];
+    totals[threadIdx.x] = before + incl - v;
 }
 
 __global__ void __launch_bounds__(kThreads) rs_downsweep(const unsigned long long* __restrict__ kin,
@@ -81,13 +86,14 @@ __global__ void __launch_bounds__(kThreads) rs_downsweep(const unsigned long lon
                                                          unsigned long long* __restrict__ kout,
                                                          unsigned int* __restrict__ vout, int n,
                                                          int shift, unsigned int mask, int nblocks,
-                                                         const unsigned int* __restrict__ offsets) {
+                                                         const unsigned int* __restrict__ offsets,
+                                                         const unsigned int* __restrict__ digit_base) {
     __shared__ unsigned int wcnt[kWarps][kBins];
     __shared__ unsigned int s_off[kBins];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) wcnt[w][threadIdx.x] = 0;
-    s_off[threadIdx.x] = offsets[threadIdx.x * nblocks + blockIdx.x];
+    s_off[threadIdx.x] = offsets[threadIdx.x * nblocks + blockIdx.x] + digit_base[threadIdx.x];
     __syncthreads();
     const int wbase = blockIdx.x * kTile + warp * 32 * kIpt;
     const unsigned int lt = (1u << lane) - 1u;
@@ -132,9 +138,10 @@ __global__ void __launch_bounds__(kThreads) rs_downsweep(const unsigned long lon
 }
 }  // namespace
 
+// tile counts (digit-major) followed by the kBins digit totals
 size_t radix_counts_size(int n) {
     const int nblocks = (n + kTile - 1) / kTile;
-    return size_t(kBins) * size_t(nblocks > 0 ? nblocks : 1);
+    return size_t(kBins) * size_t(nblocks > 0 ? nblocks : 1) + kBins;
 }
 
 cudaError_t radix_sort_pairs(unsigned long long* keys, unsigned int* vals, unsigned long long* keys_tmp,
@@ -150,9 +157,11 @@ cudaError_t radix_sort_pairs(unsigned long long* keys, unsigned int* vals, unsig
         const int shift = p * digit_bits;
         const int nb = min(digit_bits, bits - shift);
         const unsigned int mask = (1u << nb) - 1u;
+        unsigned int* totals = counts + size_t(kBins) * size_t(nblocks);
         rs_upsweep<<<nblocks, kThreads, 0, s>>>(ka, n, shift, mask, nblocks, counts);
-        rs_scan<<<1, kScanThreads, 0, s>>>(counts, kBins * nblocks);
-        rs_downsweep<<<nblocks, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, mask, nblocks, counts);
+        rs_scan_rows<<<kBins / kWarps, kThreads, 0, s>>>(counts, nblocks, totals);
+        rs_scan_digits<<<1, kBins, 0, s>>>(totals);
+        rs_downsweep<<<nblocks, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, mask, nblocks, counts, totals);
         unsigned long long* tk = ka; ka = kb; kb = tk;
         unsigned int* tv = va; va = vb; vb = tv;
     }

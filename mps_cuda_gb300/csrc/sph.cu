@@ -162,6 +162,21 @@ __global__ void k_reorder(Dev d, Params p, int n_real) {
 }
 
 // Fluid cell lookup; stale entries of cells emptied since an earlier step fail the key check.
+// Runs test(x[j], j) for j in [b, e) in order, loading kScan candidates before testing them.
+constexpr int kScan = 4;
+template <class Test>
+__device__ __forceinline__ void scan_range(const float4* __restrict__ x, unsigned b, unsigned e, Test test) {
+    unsigned j = b;
+    for (; j + kScan <= e; j += kScan) {
+        float4 v[kScan];
+#pragma unroll
+        for (int u = 0; u < kScan; ++u) v[u] = x[j + u];
+#pragma unroll
+        for (int u = 0; u < kScan; ++u) test(v[u], j + u);
+    }
+    for (; j < e; ++j) test(x[j], j);
+}
+
 __device__ __forceinline__ bool fluid_cell(const Dev& d, int slots, unsigned long long key, uint2& e) {
     e = d.ftable[key];
     return e.x < e.y && e.x < unsigned(slots) && d.slot_key[e.x] == key;
@@ -278,9 +293,10 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
                     const uint2 eb = d.btable[row + unsigned(x)];
                     if (eb.x < eb.y) { bb = min(bb, eb.x); be = max(be, eb.y); }
                 }
-                for (unsigned j = fb; j < fe; ++j) {
-                    if (j == unsigned(i)) continue;
-                    const float4 xj = d.pos[j];
+                // candidates of a row range in order, loaded kScan at a time (the loads do not
+                // depend on the tests, so a batch is in flight together)
+                auto fluid_test = [&](const float4& xj, unsigned j) {
+                    if (j == unsigned(i)) return;
                     const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
                     const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
                     if (d2 < __fmul_rn(hij, hij)) {
@@ -296,16 +312,17 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
                         }
                         nf++;
                     }
-                }
-                for (unsigned j = bb; j < be; ++j) {
-                    const float4 xj = d.bpos[j];
+                };
+                auto bnd_test = [&](const float4& xj, unsigned j) {
                     const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
                     const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
                     if (d2 < __fmul_rn(hij, hij)) {
                         if (nb < unsigned(p.cap_b)) d.nbr_b[size_t(nb) * stride + size_t(i)] = j; else over = true;
                         nb++;
                     }
-                }
+                };
+                scan_range(d.pos, fb, fe, fluid_test);
+                scan_range(d.bpos, bb, be, bnd_test);
             }
         }
         if (over) atomicOr(&d.ctr->flags, 1);

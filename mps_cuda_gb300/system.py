@@ -206,8 +206,8 @@ class Simulation:
 
     def launches_per_step(self, runs: tuple[int, int, int], radix_passes: int) -> int:
         """Kernel launches of one graph step given its loop-body counts (DF, CG, CD)."""
-        # keys + radix (3 per pass) + reorder, lists, [volume], density, DF init + condition
-        static = 2 + 3 * radix_passes + 1 + (1 if self.cfg.volume_accumulate else 0) + 1 + 2
+        # keys + radix (4 per pass) + reorder, lists, [volume], density, DF init + condition
+        static = 2 + 4 * radix_passes + 1 + (1 if self.cfg.volume_accumulate else 0) + 1 + 2
         jacobi = self.cfg.visc_solver == L.VISC_JACOBI
         # DF finish + solve set-up (+ A x0 for the CG), solve finish + CD set-up, CD finish + advect
         static += (5 if jacobi else 6) + 4 + 2
