@@ -41,6 +41,11 @@ ALGO_BYTES = {"pressure_A": 44, "pressure_B": 52, "cg_ap": 72}
 BOUNDARY_BYTES = 16
 
 
+def overrides(args) -> dict:
+    """Library config fields set on the command line."""
+    return {} if args.cg_form is None else {"cg_form": args.cg_form}
+
+
 def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -131,7 +136,7 @@ def run_ours(args, scene, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
-    sim = Simulation.from_scene(scene, device=local_rank, use_graph=0 if args.eager else 1)
+    sim = Simulation.from_scene(scene, device=local_rank, use_graph=0 if args.eager else 1, **overrides(args))
 
     def barrier():
         if dist:
@@ -553,7 +558,7 @@ def run_precision(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
     sc = scenes.colliding_4m(seed=rank, scale=args.scale)
-    sim = Simulation.from_scene(sc, device=local_rank)
+    sim = Simulation.from_scene(sc, device=local_rank, **overrides(args))
     threads = os.cpu_count() or 1
     o = orc.from_scene(sc, threads=threads)
     every = args.sample_every
@@ -609,7 +614,7 @@ def run_longrun(args, rank, world, local_rank):
     build.build()
     torch.cuda.set_device(local_rank)
     sc = scenes.dam_break_32k(seed=rank)
-    sim = Simulation.from_scene(sc, device=local_rank)
+    sim = Simulation.from_scene(sc, device=local_rank, **overrides(args))
     o = orc.from_scene(sc, threads=os.cpu_count() or 1)
     rho0 = sc.material["density"]
     m = sc.vel4[:, 3].astype(np.float64)
@@ -701,6 +706,8 @@ def main():
     ap.add_argument("--check-scenes", type=int, default=1)
     ap.add_argument("--sample-every", type=int, default=50, help="precision_4m / longrun_32k: steps between samples")
     ap.add_argument("--scale", type=float, default=1.0, help="precision_4m: block size scale (1 = 2 x 2M)")
+    ap.add_argument("--cg-form", type=int, default=None, choices=[0, 1],
+                    help="CG arrangement: 0 three-pass (the reference's, library default), 1 two-pass")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.steps is None:

@@ -84,7 +84,17 @@ typedef struct mps_config {
     int32_t stage;               /* 1: pressure passes stage neighbour data in shared memory (off by default: slower here) */
     int32_t sort_digit_bits;     /* radix digit width of the cell sort (1..8) */
     int32_t visc_solver;         /* mps_visc_solver: implicit viscosity/surface-tension solve */
+    int32_t cg_form;             /* mps_cg_form: arrangement of the CG iteration (same iterates) */
 } mps_config;
+
+/* MPS_CG_THREE_PASS (default): the reference's arrangement (MPSSolver.cuh:33-60): A p with r.r
+ * and p.Ap, then x/r update with the new r.r, then the direction update.  MPS_CG_TWO_PASS: the
+ * Chronopoulos-Gear arrangement: A r with r.r and r.w, then one vector pass updating p, s = A p
+ * (by recurrence), x and r; about 5 % faster per step.  Equal in exact arithmetic; in FP32 the
+ * recurrence for s adds rounding: against the FP64 oracle from an identical state, single
+ * particles' velocities then differ by up to ~1e-4 (max-norm) where the three-pass form stays
+ * below ~3e-6 (RMS ~2e-7 for both). */
+enum mps_cg_form { MPS_CG_THREE_PASS = 0, MPS_CG_TWO_PASS = 1 };
 
 /* MPS_VISC_CG: the reference's CGSolver (MPSSolver.cuh:12-73).  MPS_VISC_JACOBI: block-Jacobi
  * sweeps on the same system, the alternative of the reference's legacy Jacobi viscosity

@@ -27,6 +27,7 @@ PHASE_SORT, PHASE_NEIGHBORS, PHASE_BVOLUME, PHASE_DENSITY_ALPHA, PHASE_DF, PHASE
 KERNEL_POLY6_SPIKY, KERNEL_CUBIC_SPLINE = 0, 1
 K_PRESSURE_A, K_PRESSURE_B, K_CG_AP, K_DENSITY_ALPHA, K_BUILD_NBRS, K_SORT = range(6)
 VISC_CG, VISC_JACOBI = 0, 1
+CG_THREE_PASS, CG_TWO_PASS = 0, 1
 
 
 class MpsError(RuntimeError):
@@ -50,7 +51,7 @@ class Config(C.Structure):
                 ("cg_factor", C.c_double), ("fixed_iters", C.c_int32), ("max_fluid_neighbors", C.c_int32),
                 ("max_boundary_neighbors", C.c_int32), ("volume_accumulate", C.c_int32), ("use_graph", C.c_int32),
                 ("block_size", C.c_int32), ("stage", C.c_int32), ("sort_digit_bits", C.c_int32),
-                ("visc_solver", C.c_int32)]
+                ("visc_solver", C.c_int32), ("cg_form", C.c_int32)]
 
 
 class Stats(C.Structure):

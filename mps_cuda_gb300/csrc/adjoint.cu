@@ -156,6 +156,37 @@ __device__ __forceinline__ KD kern_st(float r, float invh) {
     return k;
 }
 
+// Like visit_batched, with the streamed value also passed to the gather (the reverse index of a
+// pair selects where the neighbour's coefficient is read).
+template <int B, class S, class T, class Stream, class Gather, class Use>
+__device__ __forceinline__ void visit2(const unsigned* __restrict__ list, size_t stride, int i, int n, Stream stream,
+                                       Gather gather, Use use) {
+    int k = 0;
+    for (; k + B <= n; k += B) {
+        unsigned jj[B];
+        S ss[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            jj[u] = list[size_t(k + u) * stride + size_t(i)];
+            ss[u] = stream(k + u);
+        }
+        T v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) v[u] = gather(jj[u], ss[u], k + u);
+#pragma unroll
+        for (int u = 0; u < B; ++u) use(v[u], ss[u], k + u);
+    }
+    for (; k < n; ++k) {
+        const S sk = stream(k);
+        use(gather(list[size_t(k) * stride + size_t(i)], sk, k), sk, k);
+    }
+}
+constexpr int kAdjBatch = 2;
+struct AG { float4 x, g; float k, m; };          // pass A: position, velocity cotangent, stiffness, mass
+struct BG { float4 x, u; };                      // pass B: position, velocity (w: delta cotangent)
+struct JS { float2 c; unsigned rv; };            // Jacobi reverse, streamed: own coefficient, reverse index
+struct JG { float4 x, qb, d, d2, q; float2 cji; };
+
 __device__ __forceinline__ bool slot_live(const Dev& d, int i, int& s) {
     s = d.chunk_scene[i / kChunk];
     const Scene& sc = d.scenes[s];
@@ -251,11 +282,12 @@ __global__ void __launch_bounds__(kAB) k_adj_pA(Dev d, Params p, const float4* X
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     float kbar = 0.0f;
     float3 xa = make_float3(0.f, 0.f, 0.f);
-    for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
-        const float4 xj = X[j];
-        const float kj = kap[j];
-        const float3 aj = d.vel[j].w > 1.0e-10f ? p.dt * f3(gv[j]) : make_float3(0.f, 0.f, 0.f);
+    visit2<kAdjBatch, NoStream, AG>(d.nbr_f, S, i, nf, [&](int) { return NoStream{}; },
+                                    [&](unsigned j, NoStream, int) { return AG{X[j], gv[j], kap[j], d.vel[j].w}; },
+                                    [&](const AG& t, NoStream, int) {
+        const float4 xj = t.x;
+        const float kj = t.k;
+        const float3 aj = t.m > 1.0e-10f ? p.dt * f3(t.g) : make_float3(0.f, 0.f, 0.f);
         const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
         const float r = sqrtf(dot3(e, e));
         const KD Ki = kern_d(r, invhi, p.cubic);
@@ -266,7 +298,7 @@ __global__ void __launch_bounds__(kAB) k_adj_pA(Dev d, Params p, const float4* X
         const float3 ti = Ki.G * ai + (Ki.dG * ir * aie) * e;
         const float3 tj = Kj.G * aj + (Kj.dG * ir * aje) * e;
         xa += (-0.5f * p.V * (ki + kj)) * (ti - tj);
-    }
+    });
     for (int k = 0; k < nb; ++k) {
         const unsigned b = d.nbr_b[size_t(k) * S + size_t(i)];
         const float4 xb = d.bpos[b];
@@ -309,11 +341,12 @@ __global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X
     const unsigned c = d.cnt[i];
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     float3 au = make_float3(0.f, 0.f, 0.f), xa = make_float3(0.f, 0.f, 0.f);
-    for (int k = 0; k < nf; ++k) {
-        const unsigned j = d.nbr_f[size_t(k) * S + size_t(i)];
-        const float4 xj = X[j];
-        const float dj = gdelta[j];
-        const float3 uij = ui - f3(U[j]);
+    visit2<kAdjBatch, NoStream, BG>(d.nbr_f, S, i, nf, [&](int) { return NoStream{}; },
+                                    [&](unsigned j, NoStream, int) { float4 u = U[j]; u.w = gdelta[j]; return BG{X[j], u}; },
+                                    [&](const BG& t, NoStream, int) {
+        const float4 xj = t.x;
+        const float dj = t.u.w;
+        const float3 uij = ui - f3(t.u);
         const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
         const float r = sqrtf(dot3(e, e));
         const KD Ki = kern_d(r, invhi, p.cubic);
@@ -323,7 +356,7 @@ __global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X
         const float eu = dot3(e, uij);
         xa += (p.V * di) * (Ki.G * uij + (Ki.dG * ir * eu) * e);
         xa += (p.V * dj) * (Kj.G * uij + (Kj.dG * ir * eu) * e);
-    }
+    });
     for (int k = 0; k < nb; ++k) {
         const unsigned b = d.nbr_b[size_t(k) * S + size_t(i)];
         const float4 xb = d.bpos[b];
@@ -361,32 +394,36 @@ __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float
     const float3 qi = f3(qk[i]);
     const int nf = int(d.cnt[i] & 0xffffu);
     float3 aty = (1.0f + p.cg_factor) * y;
-    for (int k = 0; k < nf; ++k) {
+    visit2<kAdjBatch, JS, JG>(d.nbr_f, S, i, nf,
+        [&](int k) { const size_t at = size_t(k) * S + size_t(i); return JS{d.cg_coef[at], unsigned(rev[at])}; },
+        [&](unsigned j, const JS& st, int) {
+            return JG{X[j], qbar[j], d.jac_d[j], d.jac_d2[j], qk[j],
+                      st.rv != 255u ? d.cg_coef[size_t(st.rv) * S + j] : make_float2(0.f, 0.f)};
+        },
+        [&](const JG& t, const JS& st, int k) {
         const size_t at = size_t(k) * S + size_t(i);
-        const unsigned j = d.nbr_f[at];
-        const float2 cij = d.cg_coef[at];
-        const float4 xj = X[j];
+        const float2 cij = st.c;
+        const float4 xj = t.x;
         const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
         const float ye = dot3(y, e);
         aty += p.dt * (cij.x * y - (cij.y * ye) * e);
-        const unsigned rv = rev[at];
-        if (rv != 255u) {
-            const float2 cji = d.cg_coef[size_t(rv) * S + j];
-            const float3 yj = sym_mul(d.jac_d[j], d.jac_d2[j], f3(qbar[j]));
+        if (st.rv != 255u) {
+            const float2 cji = t.cji;
+            const float3 yj = sym_mul(t.d, t.d2, f3(t.qb));
             const float yje = dot3(yj, e);
             aty -= p.dt * (cji.x * yj - (cji.y * yje) * e);
         }
-        const float3 pp = qi - f3(qk[j]);
+        const float3 pp = qi - f3(t.q);
         const float pe = dot3(pp, e);
         float2 a = pc[at];
         a.x += -p.dt * dot3(y, pp);
         a.y += p.dt * pe * ye;
         pc[at] = a;
         float4 b = px[at];
-        const float3 t = (p.dt * cij.y) * (pe * y + ye * pp);
-        b.x += t.x; b.y += t.y; b.z += t.z;
+        const float3 tt = (p.dt * cij.y) * (pe * y + ye * pp);
+        b.x += tt.x; b.y += tt.y; b.z += tt.z;
         px[at] = b;
-    }
+    });
     qbar_out[i] = make_float4(qb.x - aty.x, qb.y - aty.y, qb.z - aty.z, 0.0f);
     float4 bb = bbar[i];
     bb.x += y.x; bb.y += y.y; bb.z += y.z;

@@ -77,7 +77,7 @@ void mps_handle::release() {
     mpsg::host::adjoint_release(this);
     void** ptrs[] = {(void**)&pos[0], (void**)&pos[1], (void**)&vel[0], (void**)&vel[1], (void**)&ids[0],
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
-                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&nbr_l, (void**)&stage, (void**)&rho,
+                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&nbr_l, (void**)&stage, (void**)&rho, (void**)&rdev,
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol,
@@ -132,6 +132,7 @@ Params make_params(const mps_handle* h) {
     p.max_iter = c.max_iter;
     p.cg_max_iter = c.cg_max_iter;
     p.visc_solver = c.visc_solver == MPS_VISC_JACOBI ? 1 : 0;
+    p.cg_form = c.cg_form == MPS_CG_TWO_PASS ? 1 : 0;
     p.df_tol = float(c.df_tol);
     p.cd_tol = float(c.cd_tol);
     p.cg_tol = float(c.cg_tol);
@@ -165,6 +166,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.alpha = h->alpha;
     d.kappa = h->kappa;
     d.delta = h->delta;
+    d.rdev = h->rdev;
     d.aux = h->aux;
     d.color = h->color;
     d.cg_x = h->cg_x;
@@ -285,9 +287,10 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->alpha, S));
     MPS_CUDA_TRY(dalloc(&h->kappa, S));
     MPS_CUDA_TRY(dalloc(&h->delta, S));
+    MPS_CUDA_TRY(dalloc(&h->rdev, S));
     MPS_CUDA_TRY(dalloc(&h->aux, S));
     MPS_CUDA_TRY(dalloc(&h->color, S));
-    float* zf[] = {h->rho, h->alpha, h->kappa, h->delta};
+    float* zf[] = {h->rho, h->alpha, h->kappa, h->delta, h->rdev};
     for (float* z : zf) MPS_CUDA_TRY(cudaMemset(z, 0, S * sizeof(float)));
     MPS_CUDA_TRY(cudaMemset(h->aux, 0, S * sizeof(float2)));
     MPS_CUDA_TRY(cudaMemset(h->color, 0, S * sizeof(float4)));
@@ -392,9 +395,13 @@ int eager_loop(mps_handle* h, cudaStream_t s, int kind /*0 DF,1 CG,2 CD*/) {
     for (int it = 0; it < cap; ++it) {
         if (kind == 1 && p.visc_solver == 1) {
             launch_jacobi(d, p, bs, 0ull, 0, 0, nullptr, nullptr, s);
-        } else if (kind == 1) {
+        } else if (kind == 1 && p.cg_form == 1) {
             launch_cg_ap(d, p, bs, 0ull, 0, s);
             launch_cg_update(d, p, bs, 0ull, 0, 0, s);
+        } else if (kind == 1) {
+            launch_cg_ap3(d, p, bs, 0ull, 0, s);
+            launch_cg_update3(d, p, bs, s);
+            launch_cg_dir3(d, p, bs, 0ull, 0, 0, s);
         } else {
             launch_pressure_A(d, p, kind == 0 ? 0 : 1, bs, 0ull, 0, s);
             launch_pressure_B(d, p, bs, 0ull, 0, 0, s);
@@ -559,9 +566,13 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
             MPS_CAP_TRY(seg_begin(b));
             if (p.visc_solver) {
                 launch_jacobi(d, p, bs, hcg, 1, loop_limit(h, 1), nullptr, nullptr, b.s);
-            } else {
+            } else if (p.cg_form == 1) {
                 launch_cg_ap(d, p, bs, hcg, 1, b.s);
                 launch_cg_update(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+            } else {
+                launch_cg_ap3(d, p, bs, hcg, 1, b.s);
+                launch_cg_update3(d, p, bs, b.s);
+                launch_cg_dir3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
             }
             MPS_CAP_TRY(cudaGetLastError());
             MPS_CAP_TRY(seg_end(b));
@@ -723,6 +734,7 @@ void mps_default_config(mps_config* c) {
     c->stage = 0;
     c->sort_digit_bits = 8;
     c->visc_solver = MPS_VISC_CG;
+    c->cg_form = MPS_CG_THREE_PASS;
 }
 
 // SPHMaterial() + SetRadius(h): V = h^3 / 48 * 3.141592, mass = density * V
@@ -759,6 +771,7 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (h->cfg.cg_max_iter <= 0) h->cfg.cg_max_iter = 100;
     if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;
     if (h->cfg.visc_solver != MPS_VISC_JACOBI) h->cfg.visc_solver = MPS_VISC_CG;
+    if (h->cfg.cg_form != MPS_CG_TWO_PASS) h->cfg.cg_form = MPS_CG_THREE_PASS;
     *out = h;
     return MPS_OK;
 }
@@ -1080,7 +1093,9 @@ int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream
         switch (kernel) {
             case MPS_K_PRESSURE_A: launch_pressure_A(d, p, 1, bs, 0ull, 2, s); break;
             case MPS_K_PRESSURE_B: launch_pressure_B_profile(d, p, bs, s); break;
-            case MPS_K_CG_AP: launch_cg_ap(d, p, bs, 0ull, 2, s); break;
+            case MPS_K_CG_AP:
+                if (p.cg_form == 1) launch_cg_ap(d, p, bs, 0ull, 2, s); else launch_cg_ap3(d, p, bs, 0ull, 2, s);
+                break;
             case MPS_K_DENSITY_ALPHA: launch_density_alpha(d, p, bs, s); break;
             case MPS_K_BUILD_NBRS: launch_build_nbrs(d, p, bs, s); break;
             case MPS_K_SORT: {

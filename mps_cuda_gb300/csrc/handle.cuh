@@ -48,7 +48,7 @@ struct mps_handle {
     unsigned* cnt = nullptr;
     unsigned short* nbr_l = nullptr;
     mpsg::Stage* stage = nullptr;
-    float *rho = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
+    float *rho = nullptr, *rdev = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
     float2* aux = nullptr;
     float4* color = nullptr;
     float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr, *cg_s = nullptr;

@@ -79,6 +79,7 @@ struct Params {
     int fixed_iters;
     int min_iter_df, min_iter_cd, max_iter, cg_max_iter;
     int visc_solver;              // 0 CG, 1 Jacobi
+    int cg_form;                  // 0 three-pass (reference), 1 two-pass
     float df_tol, cd_tol, cg_tol; // stored as float for the kernel args; compared in FP64
     double df_tol_d, cd_tol_d, cg_tol_d;
 };
@@ -101,6 +102,7 @@ struct Dev {
     Stage* stage;                 // staging layout per thread block of the pass kernels
     int stage_on;                 // 1: pass kernels stage neighbour data in shared memory
     float* rho;
+    float* rdev;                  // rho / rho0 - 1 from the compensated sums (the stiffness reads this)
     float* alpha;
     float* kappa;
     float* delta;
@@ -287,6 +289,11 @@ void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond
                   cudaStream_t s);
 void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                       cudaStream_t s);
+// three-pass form: A p + dots, x/r update + r.r, direction update (with the loop guard)
+void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s);
+void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s);
+void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                    cudaStream_t s);
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);
 // Jacobi sweep of the viscosity/surface-tension system; src/dst null = the two iterate buffers
 // chosen by the scene's loop counter (graph form), else explicit (adjoint recording).

@@ -421,6 +421,9 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
     });
     const float rho = (rf.s + rb.s) * p.rho0;
     d.rho[i] = rho;
+    // rho / rho0 - 1 without the rounding of rho itself: rf.s - 1 is exact (Sterbenz), and the
+    // Kahan sums carry their lost low parts in c (true sum = s - c)
+    d.rdev[i] = __fsub_rn(__fadd_rn(__fsub_rn(rf.s, 1.0f), rb.s), __fadd_rn(rf.c, rb.c));
     // alpha denominator in FP64: |sum grad|^2 + sum |grad|^2, clamp at 1e-20 (MPSSPHDFSPHUtil.cuh:127-137)
     const double sx = gx.s, sy = gy.s, sz = gz.s;
     const double f = double(sq.s) + (sx * sx + sy * sy + sz * sz);
@@ -507,10 +510,11 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
             db += xj.w * g * (dx * vi.x + dy * vi.y + dz * vi.z);
         });
         const float delta = p.V * df + db;
-        const float r = d.rho[i] * p.inv_rho0;
+        // rho/rho0 + dt delta - 0.8 (DF) and rho/rho0 + dt delta - 1 (CD) from the density deviation
+        const float rd = d.rdev[i];
         const float ka = delta * p.dt;
-        const float kb = r + p.dt * delta - 0.8f;
-        float kap = mode == 0 ? fminf(ka, kb) : r + p.dt * delta - 1.0f;
+        const float kb = (rd + p.dt * delta) + 0.2f;
+        float kap = mode == 0 ? fminf(ka, kb) : rd + p.dt * delta;
         unsigned char code = 0;   // 0 clamped, 1 the dt*delta branch of DF, 2 the density branch
         if (kap > 0.0f) {
             err = kap;
@@ -769,13 +773,14 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
     return make_float3(qi.x * f1 + p.dt * sx, qi.y * f1 + p.dt * sy, qi.z * f1 + p.dt * sz);
 }
 
-// A x0 with factor 0; r = b - A x0 (MPSSolver.cuh:24-28).  The CG below runs in the
-// Chronopoulos-Gear arrangement (the same iterates as the reference's CGSolver in exact
-// arithmetic): per iteration one operator pass w = A r with the dots r.r and r.w, then one vector
-// pass p = r + beta p, s = w + beta s (s = A p), x += alpha p, r -= alpha s, where
-// beta = (r.r) / (r.r)_old and alpha = (r.r) / (r.w - beta (r.r) / alpha_old) (first iteration:
-// beta = 0, alpha = (r.r) / (r.w)).  The stop test r.r < tol and the loop counter are the
-// reference's (MPSSolver.cuh:33-60).  p and s start at zero.
+// A x0 with factor 0; r = b - A x0 (MPSSolver.cuh:24-28); p = r for the three-pass form.
+// Two-pass form (cg_form 1): the Chronopoulos-Gear arrangement (the same iterates as the
+// reference's CGSolver in exact arithmetic): per iteration one operator pass w = A r with the
+// dots r.r and r.w, then one vector pass p = r + beta p, s = w + beta s (s = A p),
+// x += alpha p, r -= alpha s, where beta = (r.r) / (r.r)_old and
+// alpha = (r.r) / (r.w - beta (r.r) / alpha_old) (first iteration: beta = 0,
+// alpha = (r.r) / (r.w)); p and s start at zero.  Both forms keep the reference's stop test
+// r.r < tol and loop counter (MPSSolver.cuh:33-60).
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
@@ -783,9 +788,14 @@ __global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
     if (i >= sc.slot_begin + sc.n) return;
     const float3 a = apply_A(d, p, i, d.cg_x, 0.0f);
     const float4 b = d.cg_b[i];
-    d.cg_r[i] = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
-    d.cg_p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    d.cg_s[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 r = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
+    d.cg_r[i] = r;
+    if (p.cg_form == 0) {
+        d.cg_p[i] = r;   // three-pass form: p0 = r0
+    } else {
+        d.cg_p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        d.cg_s[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 }
 
 // w = A r, dots r.r and r.w (FP32 per thread, FP64 across warps and blocks), the stop test and
@@ -858,6 +868,95 @@ __global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p, unsigned long
     d.cg_s[i] = sv;
     d.cg_x[i] = x;
     d.cg_r[i] = make_float4(r.x - a * sv.x, r.y - a * sv.y, r.z - a * sv.z, 0.0f);
+}
+
+// ---- three-pass form (the reference's CGSolver arrangement, MPSSolver.cuh:33-60)
+// A p, dots r.r and p.Ap, the stop test and alpha = r.r / p.Ap.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long long cond, int use_cond) {
+    __shared__ double sh[32];
+    __shared__ double2 sh2[BS / 32];
+    const int s = block_scene(d, BS);
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    float rr = 0.0f, pap = 0.0f;
+    if (i < sc.slot_begin + sc.n) {
+        const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor);
+        d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
+        const float4 r = d.cg_r[i];
+        const float4 q = d.cg_p[i];
+        rr = r.x * r.x + r.y * r.y + r.z * r.z;
+        pap = q.x * a.x + q.y * a.y + q.z * a.z;
+    }
+    const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
+    if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
+    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
+    const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
+    const double tpap = scene_partial_sum<BS>(d, sc, 1, sh);
+    if (threadIdx.x == 0) {
+        SceneSolve& S = d.solve[s];
+        const int l = S.iter;
+        const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
+        const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
+        S.err = trr;
+        S.rr = trr;
+        if (stop) {
+            S.active = 0;
+            S.do_update = 0;
+        } else {
+            S.do_update = 1;
+            S.cg_alpha = trr / tpap;
+            S.iter = l + 1;
+            if (l + 1 > cap) S.active = 0;
+        }
+        finish_scene_decision(d, p, cond, use_cond);
+    }
+}
+
+// x += alpha p, r -= alpha Ap, beta = (r.r)_new / (r.r)_old.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_update3(Dev d, Params p) {
+    __shared__ double sh[32];
+    __shared__ double2 sh2[BS / 32];
+    const int s = block_scene(d, BS);
+    if (!d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    float rr = 0.0f;
+    if (i < sc.slot_begin + sc.n) {
+        const float a = float(d.solve[s].cg_alpha);
+        float4 x = d.cg_x[i];
+        float4 r = d.cg_r[i];
+        const float4 q = d.cg_p[i];
+        const float4 ap = d.cg_ap[i];
+        x.x += a * q.x; x.y += a * q.y; x.z += a * q.z;
+        r.x -= a * ap.x; r.y -= a * ap.y; r.z -= a * ap.z;
+        d.cg_x[i] = x;
+        d.cg_r[i] = r;
+        rr = r.x * r.x + r.y * r.y + r.z * r.z;
+    }
+    const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
+    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
+    if (!last_block_of_scene<BS>(d, s, sc)) return;
+    const double t = scene_partial_sum<BS>(d, sc, 0, sh);
+    if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
+}
+
+// p = r + beta p (MPSCGKernel.cuh:196-207); the loop guard of the WHILE body.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_dir3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+    if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int s = block_scene(d, BS);
+    if (!d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    if (i >= sc.slot_begin + sc.n) return;
+    const float b = float(d.solve[s].cg_beta);
+    const float4 r = d.cg_r[i];
+    float4 q = d.cg_p[i];
+    q.x = r.x + b * q.x; q.y = r.y + b * q.y; q.z = r.z + b * q.z;
+    d.cg_p[i] = q;
 }
 
 // One block-Jacobi sweep: r = b + f x0 - (A_0 + f I) q, q' = q + D^-1 r (D: the particle's 3x3
@@ -1069,6 +1168,16 @@ void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond
 void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                       cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_update, d, p, cond, use_cond, limit);
+}
+void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_ap3, d, p, cond, use_cond);
+}
+void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_update3, d, p);
+}
+void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                    cudaStream_t s) {
+    MPSG_BS_SWITCH(bs, k_cg_dir3, d, p, cond, use_cond, limit);
 }
 void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    const float4* src, float4* dst, cudaStream_t s) {

@@ -211,7 +211,8 @@ class Simulation:
         jacobi = self.cfg.visc_solver == L.VISC_JACOBI
         # DF finish + solve set-up (+ A x0 for the CG), solve finish + CD set-up, CD finish + advect
         static += (5 if jacobi else 6) + 4 + 2
-        return static + 2 * runs[0] + (1 if jacobi else 2) * runs[1] + 2 * runs[2]
+        cg = 1 if jacobi else (2 if self.cfg.cg_form == L.CG_TWO_PASS else 3)
+        return static + 2 * runs[0] + cg * runs[1] + 2 * runs[2]
 
 
 class BatchedSimulation(Simulation):

@@ -267,3 +267,29 @@ def test_empty_boundary_and_out_of_box_particles(mps, orc):
     o.step(1)
     p, v = sim.get_fluid()
     assert rel_err(p[:, :3], o.get("pos")) < 1e-6
+
+
+@pytest.mark.parametrize("fixed", [0, 6])
+def test_cg_forms_match_oracle(mps, orc, fixed):
+    """Both arrangements of the CG iteration (three-pass as the reference, two-pass) against the
+    oracle's CG from the same state."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(10, seed=6)
+    vels = []
+    for form in (mps._lib.CG_THREE_PASS, mps._lib.CG_TWO_PASS):
+        sim = Simulation.from_scene(sc, fixed_iters=fixed, cg_form=form)
+        o = orc.from_scene(sc, config=dict(fixed_iters=fixed))
+        advance_to_density(sim, o, mps)
+        sim.phase(mps.PHASE_DF)
+        o.phase(orc.DF)
+        v = sim.get_field("vel")
+        v[:, :3] = o.get("vel")
+        sim.put_field("vel", v)
+        sim.phase(mps.PHASE_VISCST)
+        o.phase(orc.VISCST)
+        gi, oi = sim.stats()["cg_iters"], o.stats()["cg_iters"]
+        assert abs(gi - oi) <= (0 if fixed else 1), (form, gi, oi)
+        if gi == oi:
+            assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL, form
+        vels.append(sim.get_field("vel")[:, :3])
+    assert rel_err(vels[1], vels[0]) < REL
