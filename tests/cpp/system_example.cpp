@@ -1,0 +1,75 @@
+// The small dam break (10^3 fluid particles, r = 0.01, spacing 0.02, walls of a 0.5 m box) driven
+// through the C++ layer the way mps::System drives the reference's step; writes the final fluid
+// state (pos4 then vel4, float32, particle-ID order) to argv[1].
+#include <cstdio>
+#include <vector>
+
+#include "mps_system.hpp"
+
+int main(int argc, char** argv) {
+    if (argc < 3) {
+        std::fprintf(stderr, "usage: %s out.bin frames\n", argv[0]);
+        return 2;
+    }
+    const int frames = std::atoi(argv[2]);
+    try {
+        const double spacing = 0.02, r = 0.01;
+        mps::SPHMaterial mat;
+        mat.SetPhysical(4 * r, 1000.0, spacing * spacing * spacing);
+        mat.SetViscosity(0.01);
+        mat.SetXSPH(0.1);
+        mat.SetSurfaceTension(0.05);
+        mps::PhysicsParam phys;
+        phys.dt = 1.0e-3;
+        phys.gravity = {0.0, -9.81, 0.0};
+        phys.min = {0.0, 0.0, 0.0};
+        phys.max = {0.5, 0.5, 0.5};
+
+        mps::System sys;
+        sys.SetDevice(0);
+        mps_config& cfg = sys.Config();
+        cfg.kernel = MPS_KERNEL_CUBIC_SPLINE;
+        cfg.df_tol = 1.0e-3;
+        cfg.cd_tol = 1.0e-3;
+        cfg.df_min_iter = 1;
+        cfg.cd_min_iter = 2;
+        cfg.max_iter = 100;
+        sys.SetPhysics(phys);
+        sys.SetMaterial(mat);
+        sys.Initalize();
+
+        const double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {0.5, 0.5, 0.5};
+        const int64_t nb = mps_gen_box_walls(lo, hi, spacing, r, 0, nullptr);
+        std::vector<float> b4(size_t(nb) * 4);
+        mps_gen_box_walls(lo, hi, spacing, r, 0, b4.data());
+        std::vector<double> bpos(static_cast<size_t>(nb) * 3), brad(static_cast<size_t>(nb));
+        for (size_t i = 0; i < size_t(nb); ++i) {
+            for (int k = 0; k < 3; ++k) bpos[3 * i + size_t(k)] = b4[4 * i + size_t(k)];
+            brad[i] = b4[4 * i + 3];
+        }
+        sys.SetBoundary(bpos, brad);
+
+        const int n = 10 * 10 * 10;
+        std::vector<float> p4(size_t(n) * 4), v4(size_t(n) * 4);
+        mps::Check(mps_gen_block(10, 10, 10, lo, spacing, r, mat.GetMass(), 0.002, 0, p4.data(), v4.data()));
+        sys.SetFluid(p4, v4);
+
+        for (int f = 0; f < frames; ++f) sys.OnUpdate();
+        sys.SetRunning(false);
+        sys.OnUpdate();   // paused: no step
+        std::vector<float> pos, vel;
+        sys.GetFluid(pos, vel);
+        const mps_stats st = sys.GetStats();
+        std::printf("frames %llu steps %lld cd_iters %d\n", (unsigned long long)sys.GetFrame(), (long long)st.steps,
+                    st.cd_iters);
+        FILE* fp = std::fopen(argv[1], "wb");
+        if (!fp) return 3;
+        std::fwrite(pos.data(), sizeof(float), pos.size(), fp);
+        std::fwrite(vel.data(), sizeof(float), vel.size(), fp);
+        std::fclose(fp);
+    } catch (const mps::Error& e) {
+        std::fprintf(stderr, "mps error %d: %s\n", e.code(), e.what());
+        return 1;
+    }
+    return 0;
+}
