@@ -13,6 +13,8 @@ CUDA step) gets bit-identical inputs.
 - ``colliding_4m``: two 2M-particle blocks at +-1 m/s around a sampled sphere in a 4 x 2 x 2 tank.
 - ``batched_256``: 256 independent dam breaks, fluid counts log-uniform in [2k, 64k].
 - ``adjoint_16k``: 32 x 32 x 16 block in a unit box, 30 fixed solver iterations.
+- ``reference_viscosity``: mps::System::ViscosityTestScene (MPSSystem.cpp:455-551), a 5 x 5 x height
+  column, with the surface-tension scene's walls.
 
 Material of the physical configs: rest density 1000, particle volume V = spacing^3 (so the rest
 lattice sums to about rho0), mass = rho0 V, viscosity 0.01, surface tension 0.05, XSPH 0.1 (the
@@ -254,6 +256,39 @@ def reference_surface_tension(size: int = 5) -> Scene:
                  dict(pos_f64=pos, hash_cell=4 * radius, hash_size=(64, 64, 64)))
 
 
+def reference_viscosity(height: int = 300, size: int = 5) -> Scene:
+    """mps::System::ViscosityTestScene (MPSSystem.cpp:455-551, commented out in Initalize): a
+    size x size x height column with the reference's literals (0.9f, 0.001f), unit mass as the
+    scene sets it before the material's mass overrides it, box walls as in the surface-tension
+    scene (the mesh-sampled cube of the reference is not shipped)."""
+    radius = 0.1
+    f32 = lambda v: float(np.float32(v))
+    gap = radius * f32(0.9)
+    offset = f32(0.001)
+    stride = gap + gap + offset
+    lw = stride * (size - 1) + gap + gap
+    start = -lw * f32(0.5)
+    start_h = 0.0
+    lo = (start + gap - 5.5, start_h - 1.0, start + gap - 5.5)
+    hi = (start + (size - 1) * stride + gap + 5.5, start_h + (height - 1) * stride + gap + 5.5,
+          start + (size - 1) * stride + gap + 5.5)
+    mat = reference_material(4 * radius)
+    pos = [(start + x * stride + gap, start + y * stride + gap, start + z * stride + gap)
+           for y in range(height) for z in range(size) for x in range(size)]
+    pos = np.array(pos, np.float64)
+    n = pos.shape[0]
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = pos
+    pos4[:, 3] = radius
+    vel4 = np.zeros((n, 4), np.float32)
+    vel4[:, 3] = mat["mass"]
+    walls = gen_walls(lo, hi, 2 * (0.25 * mat["radius"]), 0.25 * mat["radius"])
+    phys = dict(dt=0.005, gravity=(0.0, -9.8, 0.0), min=lo, max=hi)
+    cfg = dict(kernel=L.KERNEL_POLY6_SPIKY)
+    return Scene("reference_viscosity", pos4, vel4, walls, mat, phys, cfg, 1,
+                 dict(pos_f64=pos, hash_cell=4 * radius, hash_size=(64, 64, 64)))
+
+
 CONFIGS = {
     "dam_break_32k": dam_break_32k,
     "dam_break_1m": dam_break_1m,
@@ -261,4 +296,5 @@ CONFIGS = {
     "colliding_4m": colliding_4m,
     "adjoint_16k": adjoint_16k,
     "reference_surface_tension": reference_surface_tension,
+    "reference_viscosity": reference_viscosity,
 }

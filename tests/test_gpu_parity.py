@@ -293,3 +293,17 @@ def test_cg_forms_match_oracle(mps, orc, fixed):
             assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL, form
         vels.append(sim.get_field("vel")[:, :3])
     assert rel_err(vels[1], vels[0]) < REL
+
+
+def test_reference_viscosity_scene_step(mps, orc):
+    """The reference's viscosity column scene (ViscosityTestScene) with its shipped settings."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.reference_viscosity(height=20)
+    sim = Simulation.from_scene(sc, fixed_iters=4)
+    o = orc.from_scene(sc, config=dict(fixed_iters=4))
+    for _ in range(3):
+        sim.step(1)
+        o.step(1)
+    p, v = sim.get_fluid()
+    assert rel_err(p[:, :3], o.get("pos")) < 1e-5
+    assert rel_err(v[:, :3], o.get("vel")) < 1e-4
