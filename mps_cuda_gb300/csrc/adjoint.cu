@@ -22,9 +22,11 @@
 // y = D^-1 qbar, qbar -= (A_0 + f I)^T y (D symmetric).  A pair whose reverse entry is missing
 // (asymmetric lists, only after a capacity overflow) is skipped and the call reports it.
 //
-// Memory: checkpoints of the slot-order state every `every` steps, the start states of one
-// segment, and one step's tape (K + 1 velocity fields per pressure solve, K + 1 Jacobi iterates,
-// stiffness and branch codes), plus per-pair cotangents of the solve's coefficients.
+// Memory: checkpoints of the slot-order state every `every` steps and the tapes of one segment:
+// per step, K + 1 velocity fields per pressure solve, K + 1 Jacobi iterates, stiffness and branch
+// codes, and the step's neighbour lists / solve coefficients / densities the reverse reads; plus
+// per-pair cotangents of the solve's coefficients.  The reverse sweep records a segment once from
+// its checkpoint (eager, bit-identical to the graph step) and then reverses its steps.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -52,14 +54,18 @@ struct AdjointStore {
     unsigned* fin_ids = nullptr;
     int fin_cur = 0;
     int64_t fin_steps = 0;
-    // start states of the steps of one segment
-    float4 *seg_pos = nullptr, *seg_vel = nullptr;
-    unsigned* seg_ids = nullptr;
-    std::vector<int> seg_cur;
-    // one step's tape
+    // the tapes of the steps of one segment (every_cap slots, each field laid out slot after slot):
+    // velocities before each pressure iteration and after the solve, Jacobi iterates, positions,
+    // stiffness and branch codes, collision codes, and the step's neighbour lists, solve
+    // coefficients, Jacobi blocks, densities and alphas that the reverse kernels read
     float4 *t_udf = nullptr, *t_ucd = nullptr, *t_q = nullptr, *t_x = nullptr;
     float *t_kdf = nullptr, *t_kcd = nullptr;
     unsigned char *t_cdf = nullptr, *t_ccd = nullptr, *t_adv = nullptr;
+    unsigned *t_nbrf = nullptr, *t_nbrb = nullptr, *t_cnt = nullptr, *t_ids = nullptr;
+    float2 *t_coef = nullptr, *t_aux = nullptr;
+    float4 *t_jd = nullptr, *t_jd2 = nullptr;
+    float *t_rho = nullptr, *t_alpha = nullptr;
+    int capb = 0;
     // cotangents
     float4 *gx = nullptr, *gv = nullptr, *gx_id = nullptr, *gv_id = nullptr;
     float4 *qbar0 = nullptr, *qbar1 = nullptr, *bbar = nullptr, *gg = nullptr;
@@ -74,8 +80,9 @@ struct AdjointStore {
     StepCounters* ctr_save = nullptr;
 
     void free_all() {
-        void* ptrs[] = {cp_pos, cp_vel, cp_ids, fin_pos, fin_vel, fin_ids, seg_pos, seg_vel, seg_ids, t_udf, t_ucd,
-                        t_q, t_x, t_kdf, t_kcd, t_cdf, t_ccd, t_adv, gx, gv, gx_id, gv_id, qbar0, qbar1, bbar,
+        void* ptrs[] = {cp_pos, cp_vel, cp_ids, fin_pos, fin_vel, fin_ids, t_udf, t_ucd, t_q, t_x, t_kdf, t_kcd,
+                        t_cdf, t_ccd, t_adv, t_nbrf, t_nbrb, t_cnt, t_ids, t_coef, t_aux, t_jd, t_jd2, t_rho,
+                        t_alpha, gx, gv, gx_id, gv_id, qbar0, qbar1, bbar,
                         Dbar, Dbar2, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
         for (void* q : ptrs)
             if (q) cudaFree(q);
@@ -786,11 +793,15 @@ int nb_of(int n) { return (n + kAB - 1) / kAB; }
 
 size_t store_bytes(const mps_handle* h, int nsteps, int every) {
     const size_t S = size_t(h->slots), cap = size_t(h->cfg.max_fluid_neighbors), K = size_t(h->cfg.fixed_iters);
+    const size_t capb = size_t(h->cfg.max_boundary_neighbors), E = size_t(every);
     const size_t ncp = size_t((nsteps + every - 1) / every);
     const size_t state = S * (2 * sizeof(float4) + sizeof(unsigned));
-    size_t b = (ncp + 1 + size_t(every)) * state;
-    b += (3 * (K + 1) + 1) * S * sizeof(float4);            // tapes u (DF, CD), q, x
-    b += 2 * K * S * (sizeof(float) + 1) + S;               // stiffness, codes, collision codes
+    size_t b = (ncp + 1) * state;
+    size_t step = (3 * (K + 1) + 1) * S * sizeof(float4);               // tapes u (DF, CD), q, x
+    step += 2 * K * S * (sizeof(float) + 1) + S;                         // stiffness, codes, collision codes
+    step += (cap + capb + 2) * S * sizeof(unsigned) + cap * S * sizeof(float2);   // lists, counts, ids, coefficients
+    step += S * (sizeof(float2) + 2 * sizeof(float4) + 2 * sizeof(float));      // aux, Jacobi blocks, rho, alpha
+    b += E * step;
     b += 10 * S * sizeof(float4) + 4 * S * sizeof(float) + 2 * S * sizeof(double);   // cotangents
     b += cap * S * (sizeof(float2) + sizeof(float4) + 1);   // per-pair cotangents + reverse index
     b += size_t(h->nscenes) * 2 * sizeof(double) + 64;
@@ -817,9 +828,10 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     A.ncp_cap = ncp;
     A.every_cap = every;
     A.cap = h->cfg.max_fluid_neighbors;
+    A.capb = h->cfg.max_boundary_neighbors;
     A.nscenes = h->nscenes;
     A.n = h->n;
-    const size_t S = size_t(h->slots), cap = size_t(A.cap);
+    const size_t S = size_t(h->slots), cap = size_t(A.cap), capb = size_t(A.capb), E = size_t(every);
     size_t& t = A.bytes;
     ADJ_TRY(alloc(&A.cp_pos, S * ncp, t));
     ADJ_TRY(alloc(&A.cp_vel, S * ncp, t));
@@ -827,18 +839,25 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     ADJ_TRY(alloc(&A.fin_pos, S, t));
     ADJ_TRY(alloc(&A.fin_vel, S, t));
     ADJ_TRY(alloc(&A.fin_ids, S, t));
-    ADJ_TRY(alloc(&A.seg_pos, S * every, t));
-    ADJ_TRY(alloc(&A.seg_vel, S * every, t));
-    ADJ_TRY(alloc(&A.seg_ids, S * every, t));
-    ADJ_TRY(alloc(&A.t_udf, S * (K + 1), t));
-    ADJ_TRY(alloc(&A.t_ucd, S * (K + 1), t));
-    ADJ_TRY(alloc(&A.t_q, S * (K + 1), t));
-    ADJ_TRY(alloc(&A.t_x, S, t));
-    ADJ_TRY(alloc(&A.t_kdf, S * K, t));
-    ADJ_TRY(alloc(&A.t_kcd, S * K, t));
-    ADJ_TRY(alloc(&A.t_cdf, S * K, t));
-    ADJ_TRY(alloc(&A.t_ccd, S * K, t));
-    ADJ_TRY(alloc(&A.t_adv, S, t));
+    ADJ_TRY(alloc(&A.t_udf, E * S * (K + 1), t));
+    ADJ_TRY(alloc(&A.t_ucd, E * S * (K + 1), t));
+    ADJ_TRY(alloc(&A.t_q, E * S * (K + 1), t));
+    ADJ_TRY(alloc(&A.t_x, E * S, t));
+    ADJ_TRY(alloc(&A.t_kdf, E * S * K, t));
+    ADJ_TRY(alloc(&A.t_kcd, E * S * K, t));
+    ADJ_TRY(alloc(&A.t_cdf, E * S * K, t));
+    ADJ_TRY(alloc(&A.t_ccd, E * S * K, t));
+    ADJ_TRY(alloc(&A.t_adv, E * S, t));
+    ADJ_TRY(alloc(&A.t_nbrf, E * S * cap, t));
+    ADJ_TRY(alloc(&A.t_nbrb, E * S * capb, t));
+    ADJ_TRY(alloc(&A.t_cnt, E * S, t));
+    ADJ_TRY(alloc(&A.t_ids, E * S, t));
+    ADJ_TRY(alloc(&A.t_coef, E * S * cap, t));
+    ADJ_TRY(alloc(&A.t_aux, E * S, t));
+    ADJ_TRY(alloc(&A.t_jd, E * S, t));
+    ADJ_TRY(alloc(&A.t_jd2, E * S, t));
+    ADJ_TRY(alloc(&A.t_rho, E * S, t));
+    ADJ_TRY(alloc(&A.t_alpha, E * S, t));
     float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.Dbar2, &A.gg};
     for (float4** q : f4) ADJ_TRY(alloc(q, S, t));
     ADJ_TRY(alloc(&A.gx_id, size_t(std::max<int64_t>(h->n, 1)), t));
@@ -854,7 +873,6 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     ADJ_TRY(alloc(&A.flag, 1, t));
     ADJ_TRY(alloc(&A.ctr_save, 1, t));
     A.cp_cur.assign(size_t(ncp), 0);
-    A.seg_cur.assign(size_t(every), 0);
     // zero what the kernels read before writing (padding slots of the cotangents)
     for (float4** q : f4) ADJ_TRY(cudaMemset(*q, 0, S * sizeof(float4)));
     for (float** q : f1) ADJ_TRY(cudaMemset(*q, 0, S * sizeof(float)));
@@ -875,6 +893,41 @@ cudaError_t copy_state(mps_handle* h, int buf, float4* pos, float4* vel, unsigne
     if ((e = cudaMemcpyAsync(h->pos[buf], pos, S * sizeof(float4), k, s))) return e;
     if ((e = cudaMemcpyAsync(h->vel[buf], vel, S * sizeof(float4), k, s))) return e;
     return cudaMemcpyAsync(h->ids[buf], ids, S * sizeof(unsigned), k, s);
+}
+
+// The tape of step k of the current segment.
+struct Slot {
+    float4 *udf, *ucd, *q, *x;
+    float *kdf, *kcd;
+    unsigned char *cdf, *ccd, *adv;
+    unsigned *nbrf, *nbrb, *cnt, *ids;
+    float2 *coef, *aux;
+    float4 *jd, *jd2;
+    float *rho, *alpha;
+};
+Slot slot_of(const AdjointStore& A, int k) {
+    const size_t S = size_t(A.slots), K = size_t(A.K), kk = size_t(k);
+    Slot t;
+    t.udf = A.t_udf + kk * S * (K + 1);
+    t.ucd = A.t_ucd + kk * S * (K + 1);
+    t.q = A.t_q + kk * S * (K + 1);
+    t.x = A.t_x + kk * S;
+    t.kdf = A.t_kdf + kk * S * K;
+    t.kcd = A.t_kcd + kk * S * K;
+    t.cdf = A.t_cdf + kk * S * K;
+    t.ccd = A.t_ccd + kk * S * K;
+    t.adv = A.t_adv + kk * S;
+    t.nbrf = A.t_nbrf + kk * S * size_t(A.cap);
+    t.nbrb = A.t_nbrb + kk * S * size_t(A.capb);
+    t.cnt = A.t_cnt + kk * S;
+    t.ids = A.t_ids + kk * S;
+    t.coef = A.t_coef + kk * S * size_t(A.cap);
+    t.aux = A.t_aux + kk * S;
+    t.jd = A.t_jd + kk * S;
+    t.jd2 = A.t_jd2 + kk * S;
+    t.rho = A.t_rho + kk * S;
+    t.alpha = A.t_alpha + kk * S;
+    return t;
 }
 
 // One pressure solve recorded: u^k before each iteration, kappa^k and the branch codes.
@@ -899,59 +952,87 @@ int taped_pressure(mps_handle* h, int mode, float4* tu, float* tk, unsigned char
     return MPS_OK;
 }
 
-// The step of mps_step, run phase by phase with recording (bit-identical to the plain step).
-int taped_step(mps_handle* h, cudaStream_t s) {
+template <class T>
+cudaError_t save(T* dst, const T* src, size_t count, cudaStream_t s) {
+    return cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToDevice, s);
+}
+
+// The step of mps_step, run phase by phase with recording into slot t (bit-identical to the
+// plain step); the handle advances to the step's output.
+int taped_step(mps_handle* h, const Slot& t, cudaStream_t s) {
     AdjointStore& A = *h->adj;
+    const size_t S = size_t(h->slots);
     int r;
     if ((r = host::run_phase(h, MPS_PHASE_SORT, s))) return r;
     if ((r = host::run_phase(h, MPS_PHASE_NEIGHBORS, s))) return r;
     if ((r = host::run_phase(h, MPS_PHASE_BVOLUME, s))) return r;
     if ((r = host::run_phase(h, MPS_PHASE_DENSITY_ALPHA, s))) return r;
-    if ((r = taped_pressure(h, 0, A.t_udf, A.t_kdf, A.t_cdf, s))) return r;
+    if ((r = taped_pressure(h, 0, t.udf, t.kdf, t.cdf, s))) return r;
     {
         const Params p = host::make_params(h);
         const Dev d = host::make_dev(h, h->cur);
         const int bs = host::block_size(h);
-        const size_t S = size_t(h->slots);
         launch_st_factor(d, p, bs, s);
         launch_cg_b(d, p, bs, s);
-        ADJ_TRY(cudaMemcpyAsync(A.t_q, h->cg_x, S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+        ADJ_TRY(save(t.q, h->cg_x, S, s));
         launch_solver_init(d, p, s);
         for (int k = 0; k < A.K; ++k)
-            launch_jacobi(d, p, bs, 0ull, 0, 0, A.t_q + size_t(k) * S, A.t_q + size_t(k + 1) * S, s);
+            launch_jacobi(d, p, bs, 0ull, 0, 0, t.q + size_t(k) * S, t.q + size_t(k + 1) * S, s);
         launch_solver_finish(d, p, 1, s);
-        launch_jacobi_finish(d, p, A.t_q + size_t(A.K) * S, s);
+        launch_jacobi_finish(d, p, t.q + size_t(A.K) * S, s);
         ADJ_TRY(cudaGetLastError());
     }
-    if ((r = taped_pressure(h, 1, A.t_ucd, A.t_kcd, A.t_ccd, s))) return r;
+    if ((r = taped_pressure(h, 1, t.ucd, t.kcd, t.ccd, s))) return r;
     {
         const Params p = host::make_params(h);
         Dev d = host::make_dev(h, h->cur);
-        ADJ_TRY(cudaMemcpyAsync(A.t_x, h->pos[h->cur], size_t(h->slots) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
-        d.tape_adv = A.t_adv;
+        ADJ_TRY(save(t.x, h->pos[h->cur], S, s));
+        d.tape_adv = t.adv;
         launch_advect(d, p, s);
         ADJ_TRY(cudaGetLastError());
     }
+    // what the reverse kernels read of this step
+    ADJ_TRY(save(t.nbrf, h->nbr_f, S * size_t(A.cap), s));
+    ADJ_TRY(save(t.nbrb, h->nbr_b, S * size_t(A.capb), s));
+    ADJ_TRY(save(t.cnt, h->cnt, S, s));
+    ADJ_TRY(save(t.ids, h->ids[h->cur], S, s));
+    ADJ_TRY(save(t.coef, h->cg_coef, S * size_t(A.cap), s));
+    ADJ_TRY(save(t.aux, h->aux, S, s));
+    ADJ_TRY(save(t.jd, h->cg_ap, S, s));
+    ADJ_TRY(save(t.jd2, h->cg_r, S, s));
+    ADJ_TRY(save(t.rho, h->rho, S, s));
+    ADJ_TRY(save(t.alpha, h->alpha, S, s));
     return MPS_OK;
 }
 
-// Reverse of the step just recorded: cotangents of its output (ID order, A.gx_id / A.gv_id) are
-// replaced by those of its input.
-int adjoint_step(mps_handle* h, cudaStream_t s) {
+// Reverse of the step recorded in slot t: cotangents of its output (ID order, A.gx_id / A.gv_id)
+// are replaced by those of its input.
+int adjoint_step(mps_handle* h, const Slot& t, cudaStream_t s) {
     AdjointStore& A = *h->adj;
     const Params p = host::make_params(h);
-    const Dev d = host::make_dev(h, h->cur);
+    Dev d = host::make_dev(h, h->cur);
+    d.nbr_f = t.nbrf;
+    d.nbr_b = t.nbrb;
+    d.cnt = t.cnt;
+    d.ids = t.ids;
+    d.cg_coef = t.coef;
+    d.aux = t.aux;
+    d.jac_d = t.jd;
+    d.jac_d2 = t.jd2;
+    d.rho = t.rho;
+    d.alpha = t.alpha;
+    d.vel = t.udf;   // masses (w) in slot order of this step
     const size_t S = size_t(h->slots), cap = size_t(A.cap);
     const int K = A.K;
     const int nb = nb_of(h->slots);
     k_adj_gather<<<nb, kAB, 0, s>>>(d, p, A.gx_id, A.gv_id, A.gx, A.gv, A.grho, A.galpha);
     k_adj_rev<<<nb, kAB, 0, s>>>(d, p, A.rev, A.flag);
-    k_adj_advect<<<nb, kAB, 0, s>>>(d, p, A.t_adv, A.gx, A.gv);
+    k_adj_advect<<<nb, kAB, 0, s>>>(d, p, t.adv, A.gx, A.gv);
     // constant-density solve
     for (int k = K - 1; k >= 0; --k) {
-        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_kcd + size_t(k) * S, A.t_ccd + size_t(k) * S, A.gv, A.gdelta,
+        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, t.x, t.kcd + size_t(k) * S, t.ccd + size_t(k) * S, A.gv, A.gdelta,
                                      A.grho, A.galpha, A.gx);
-        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_ucd + size_t(k) * S, A.gdelta, A.gv, A.gx);
+        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, t.x, t.ucd + size_t(k) * S, A.gdelta, A.gv, A.gx);
     }
     // viscosity + surface tension (Jacobi)
     ADJ_TRY(cudaMemsetAsync(A.pc, 0, cap * S * sizeof(float2), s));
@@ -963,24 +1044,27 @@ int adjoint_step(mps_handle* h, cudaStream_t s) {
     float4* qa = A.qbar0;
     float4* qb = A.qbar1;
     for (int k = K - 1; k >= 0; --k) {
-        k_adj_jacobi<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.rev, A.t_q + size_t(k) * S, A.t_q + size_t(k + 1) * S, qa, qb,
+        k_adj_jacobi<<<nb, kAB, 0, s>>>(d, p, t.x, A.rev, t.q + size_t(k) * S, t.q + size_t(k + 1) * S, qa, qb,
                                          A.bbar, A.Dbar, A.Dbar2, A.pc, A.px);
         std::swap(qa, qb);
     }
-    const float4* V0 = A.t_udf + size_t(K) * S;   // pre-solve velocity = DF output
-    k_adj_visc_coef<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.rev, qa, A.bbar, A.Dbar, A.Dbar2, A.pc, A.px, A.gv, A.gx,
+    const float4* V0 = t.udf + size_t(K) * S;   // pre-solve velocity = DF output
+    k_adj_visc_coef<<<nb, kAB, 0, s>>>(d, p, t.x, V0, A.rev, qa, A.bbar, A.Dbar, A.Dbar2, A.pc, A.px, A.gv, A.gx,
                                         A.grho, A.gsf, A.gsig, A.gmu);
-    k_adj_stfac<<<nb, kAB, 0, s>>>(d, p, A.t_x, V0, A.gsf, A.gv, A.gx);
+    k_adj_stfac<<<nb, kAB, 0, s>>>(d, p, t.x, V0, A.gsf, A.gv, A.gx);
     // divergence-free solve
     for (int k = K - 1; k >= 0; --k) {
-        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_kdf + size_t(k) * S, A.t_cdf + size_t(k) * S, A.gv, A.gdelta,
+        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, t.x, t.kdf + size_t(k) * S, t.cdf + size_t(k) * S, A.gv, A.gdelta,
                                      A.grho, A.galpha, A.gx);
-        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.t_udf + size_t(k) * S, A.gdelta, A.gv, A.gx);
+        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, t.x, t.udf + size_t(k) * S, A.gdelta, A.gv, A.gx);
     }
     // gravity is the identity; density and alpha
-    k_adj_dens_a<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.galpha, A.gg);
-    k_adj_dens_b<<<nb, kAB, 0, s>>>(d, p, A.t_x, A.grho, A.gg, A.gx);
+    k_adj_dens_a<<<nb, kAB, 0, s>>>(d, p, t.x, A.galpha, A.gg);
+    k_adj_dens_b<<<nb, kAB, 0, s>>>(d, p, t.x, A.grho, A.gg, A.gx);
     k_adj_scatter<<<nb, kAB, 0, s>>>(d, p, A.gx, A.gv, A.gx_id, A.gv_id);
+    k_adj_param_reduce<<<h->nscenes, 256, 0, s>>>(d, p, A.gsig, A.gmu, A.gparam);
+    ADJ_TRY(cudaMemsetAsync(A.gsig, 0, S * sizeof(double), s));
+    ADJ_TRY(cudaMemsetAsync(A.gmu, 0, S * sizeof(double), s));
     ADJ_TRY(cudaGetLastError());
     return MPS_OK;
 }
@@ -1071,33 +1155,16 @@ int mps_adjoint_backward(mps_handle* h, const float* g_pos4, const float* g_vel4
     ADJ_TRY(cudaMemsetAsync(A.gparam, 0, 2 * size_t(h->nscenes) * sizeof(double), s));
     ADJ_TRY(cudaMemsetAsync(A.flag, 0, sizeof(int), s));
     const int nseg = (A.nsteps + A.every - 1) / A.every;
-    const Params p = host::make_params(h);
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int t0 = seg * A.every, t1 = std::min(A.nsteps, t0 + A.every);
-        // start states of the segment's steps, recomputed from the checkpoint with the plain step
+        // record the segment's steps from its checkpoint, then reverse them
         h->cur = A.cp_cur[size_t(seg)];
         ADJ_TRY(copy_state(h, h->cur, A.cp_pos + size_t(seg) * S, A.cp_vel + size_t(seg) * S, A.cp_ids + size_t(seg) * S,
                            false, s));
-        for (int t = t0; t < t1; ++t) {
-            const int k = t - t0;
-            ADJ_TRY(copy_state(h, h->cur, A.seg_pos + size_t(k) * S, A.seg_vel + size_t(k) * S, A.seg_ids + size_t(k) * S,
-                               true, s));
-            A.seg_cur[size_t(k)] = h->cur;
-            if (t + 1 < t1 && (r = host::step_n(h, 1, s))) return r;
-        }
-        for (int t = t1 - 1; t >= t0; --t) {
-            const int k = t - t0;
-            h->cur = A.seg_cur[size_t(k)];
-            ADJ_TRY(copy_state(h, h->cur, A.seg_pos + size_t(k) * S, A.seg_vel + size_t(k) * S, A.seg_ids + size_t(k) * S,
-                               false, s));
-            if ((r = taped_step(h, s))) return r;
-            if ((r = adjoint_step(h, s))) return r;
-            const Dev d = host::make_dev(h, h->cur);
-            k_adj_param_reduce<<<h->nscenes, 256, 0, s>>>(d, p, A.gsig, A.gmu, A.gparam);
-            ADJ_TRY(cudaMemsetAsync(A.gsig, 0, S * sizeof(double), s));
-            ADJ_TRY(cudaMemsetAsync(A.gmu, 0, S * sizeof(double), s));
-            ADJ_TRY(cudaGetLastError());
-        }
+        for (int k = 0; k < t1 - t0; ++k)
+            if ((r = taped_step(h, slot_of(A, k), s))) return r;
+        for (int k = t1 - t0 - 1; k >= 0; --k)
+            if ((r = adjoint_step(h, slot_of(A, k), s))) return r;
     }
     int flag = 0, ctr_flags = 0;
     ADJ_TRY(cudaMemcpyAsync(&flag, A.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
