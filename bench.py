@@ -213,8 +213,9 @@ def run_ours(args, scene, rank, world, local_rank):
             traffic = d.get("bytes_per_launch_full_workload")
     step_algo = (432 + 96 * (runs[0] + runs[2]) / args.steps + 184 * runs[1] / args.steps) * scene.n + \
         16 * scene.nb * (1 + 2 * (runs[0] + runs[2]) / args.steps)
+    metric = METRIC if scene.name == "dam_break_1m" else f"particle-steps/s (DFSPH, {scene.name})"
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,
@@ -671,7 +672,7 @@ def run_reference(args, scene, rank, world, local_rank):
     value = scene.n * args.steps / dt
     loops = ref.loops()
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "impl": "reference", "metric": METRIC if scene.name == "dam_break_1m" else f"particle-steps/s (DFSPH, {scene.name})", "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,

@@ -436,7 +436,6 @@ int run_phase(mps_handle* h, int phase, cudaStream_t s) {
             const Dev d = make_dev(h, h->cur);
             launch_st_factor(d, p, bs, s);
             launch_cg_b(d, p, bs, s);
-            if (!p.visc_solver) launch_cg_ax0(d, p, bs, s);
             launch_solver_init(d, p, s);
             const int r = eager_loop(h, s, 1);
             if (r) return r;
@@ -555,7 +554,6 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         launch_solver_finish(d, p, 0, c.s);
         launch_st_factor(d, p, bs, c.s);
         launch_cg_b(d, p, bs, c.s);
-        if (!p.visc_solver) launch_cg_ax0(d, p, bs, c.s);
         launch_solver_init(d, p, c.s);
         launch_set_cond(d, hcg, c.s);
         MPS_CAP_TRY(cudaGetLastError());

@@ -284,7 +284,6 @@ void launch_pressure_B_profile(const Dev& d, const Params& p, int bs, cudaStream
 void launch_solver_finish(const Dev& d, const Params& p, int which, cudaStream_t s);
 void launch_st_factor(const Dev& d, const Params& p, int bs, cudaStream_t s);
 void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s);
-void launch_cg_ax0(const Dev& d, const Params& p, int bs, cudaStream_t s);
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond,
                   cudaStream_t s);
 void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,

@@ -698,6 +698,7 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     const int nf = int(d.cnt[i] & 0xffffu);
     float bx = 0.0f, by = 0.0f, bz = 0.0f;
     float csum = 0.0f, sxx = 0.0f, syy = 0.0f, szz = 0.0f, sxy = 0.0f, sxz = 0.0f, syz = 0.0f;  // Jacobi block sums
+    float ax = 0.0f, ay = 0.0f, az = 0.0f;   // sum of the operator's pair terms applied to x0 = v
     visit_batched<MPSG_B_SETUP, NoStream, XVA>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
                        [&](unsigned j, int) { return XVA{d.pos[j], d.vel[j], d.aux[j]}; },
                        [&](const XVA& t, NoStream, int k) {
@@ -725,9 +726,27 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
         csum += cf.x;
         sxx += cf.y * dx * dx; syy += cf.y * dy * dy; szz += cf.y * dz * dz;
         sxy += cf.y * dx * dy; sxz += cf.y * dx * dz; syz += cf.y * dy * dz;
+        // apply_A's pair term on x0 = v with these coefficients (the CG's A x0, factor 0)
+        const float px = vi.x - vj.x, py = vi.y - vj.y, pz = vi.z - vj.z;
+        const float tt = cf.y * (px * dx + py * dy + pz * dz);
+        ax += cf.x * px - tt * dx;
+        ay += cf.x * py - tt * dy;
+        az += cf.x * pz - tt * dz;
     });
-    d.cg_b[i] = make_float4(vi.x + st_scale * bx, vi.y + st_scale * by, vi.z + st_scale * bz, 0.0f);
+    const float4 b = make_float4(vi.x + st_scale * bx, vi.y + st_scale * by, vi.z + st_scale * bz, 0.0f);
+    d.cg_b[i] = b;
     d.cg_x[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
+    if (p.visc_solver == 0) {
+        // r0 = b - A x0 with factor 0 (MPSSolver.cuh:24-28); p0 = r0 (three-pass form) or p = s = 0
+        const float4 r = make_float4(b.x - (vi.x + p.dt * ax), b.y - (vi.y + p.dt * ay), b.z - (vi.z + p.dt * az), 0.0f);
+        d.cg_r[i] = r;
+        if (p.cg_form == 0) {
+            d.cg_p[i] = r;
+        } else {
+            d.cg_p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d.cg_s[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
     if (p.visc_solver == 1) {
         // 3x3 diagonal block of A_0 + f I, (1 + f + dt sum c) I - dt sum cv x x^T, inverted by
         // cofactors; a block with det <= 1e-30 (or not finite) is replaced by (1 + f) I and flagged
@@ -773,33 +792,13 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
     return make_float3(qi.x * f1 + p.dt * sx, qi.y * f1 + p.dt * sy, qi.z * f1 + p.dt * sz);
 }
 
-// A x0 with factor 0; r = b - A x0 (MPSSolver.cuh:24-28); p = r for the three-pass form.
-// Two-pass form (cg_form 1): the Chronopoulos-Gear arrangement (the same iterates as the
+// Two-pass CG form (cg_form 1): the Chronopoulos-Gear arrangement (the same iterates as the
 // reference's CGSolver in exact arithmetic): per iteration one operator pass w = A r with the
 // dots r.r and r.w, then one vector pass p = r + beta p, s = w + beta s (s = A p),
 // x += alpha p, r -= alpha s, where beta = (r.r) / (r.r)_old and
 // alpha = (r.r) / (r.w - beta (r.r) / alpha_old) (first iteration: beta = 0,
 // alpha = (r.r) / (r.w)); p and s start at zero.  Both forms keep the reference's stop test
-// r.r < tol and loop counter (MPSSolver.cuh:33-60).
-template <int BS>
-__global__ void __launch_bounds__(BS) k_cg_ax0(Dev d, Params p) {
-    const int i = blockIdx.x * BS + threadIdx.x;
-    const Scene& sc = d.scenes[block_scene(d, BS)];
-    if (i >= sc.slot_begin + sc.n) return;
-    const float3 a = apply_A(d, p, i, d.cg_x, 0.0f);
-    const float4 b = d.cg_b[i];
-    const float4 r = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
-    d.cg_r[i] = r;
-    if (p.cg_form == 0) {
-        d.cg_p[i] = r;   // three-pass form: p0 = r0
-    } else {
-        d.cg_p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        d.cg_s[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-}
-
-// w = A r, dots r.r and r.w (FP32 per thread, FP64 across warps and blocks), the stop test and
-// the step coefficients (MPSSolver.cuh:33-49 in the Chronopoulos-Gear arrangement).
+// r.r < tol and loop counter (MPSSolver.cuh:33-60); r0 = b - A x0 comes from k_cg_b.
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long long cond, int use_cond) {
     __shared__ double sh[32];
@@ -1159,25 +1158,28 @@ void launch_st_factor(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_b, d, p);
 }
-void launch_cg_ax0(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_ax0, d, p);
-}
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
 }
+// The CG's vector passes stream their arrays; they run with 256-thread blocks whatever the
+// neighbour passes use (half the per-block partials for the residual sums; scenes are padded to
+// 256 slots, so a block still belongs to one scene).
 void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                       cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_update, d, p, cond, use_cond, limit);
+    (void)bs;
+    MPSG_BS_SWITCH(256, k_cg_update, d, p, cond, use_cond, limit);
 }
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap3, d, p, cond, use_cond);
 }
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_update3, d, p);
+    (void)bs;
+    MPSG_BS_SWITCH(256, k_cg_update3, d, p);
 }
 void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_dir3, d, p, cond, use_cond, limit);
+    (void)bs;
+    MPSG_BS_SWITCH(256, k_cg_dir3, d, p, cond, use_cond, limit);
 }
 void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    const float4* src, float4* dst, cudaStream_t s) {

@@ -209,8 +209,9 @@ class Simulation:
         # keys + radix (4 per pass) + reorder, lists, [volume], density, DF init + condition
         static = 2 + 4 * radix_passes + 1 + (1 if self.cfg.volume_accumulate else 0) + 1 + 2
         jacobi = self.cfg.visc_solver == L.VISC_JACOBI
-        # DF finish + solve set-up (+ A x0 for the CG), solve finish + CD set-up, CD finish + advect
-        static += (5 if jacobi else 6) + 4 + 2
+        # DF finish + solve set-up (ST factor, coefficients + r0, init, condition), solve finish +
+        # CD set-up, CD finish + advect
+        static += 5 + 4 + 2
         cg = 1 if jacobi else (2 if self.cfg.cg_form == L.CG_TWO_PASS else 3)
         return static + 2 * runs[0] + cg * runs[1] + 2 * runs[2]
 
