@@ -296,3 +296,22 @@ def test_autograd_rollout_and_com_loss(mps):
     op, ov, par = roll.backward(g4x, g4v)
     assert np.allclose(v0.grad.numpy(), ov[:, :3], rtol=0, atol=1e-12)
     assert abs(float(mu.grad) - par[0, 0]) <= 1e-12 * max(1.0, abs(par[0, 0]))
+
+
+@pytest.mark.gpu
+def test_adjoint_poly6_kernel_matches_host_gradient(mps):
+    """The reference's shipped kernel pair (poly6 W, spiky gradient)."""
+    from oracle import adjoint_ref as A
+    sc = small_scene(mps, seed=12)
+    sc.config["kernel"] = mps.KERNEL_POLY6_SPIKY
+    rng = np.random.default_rng(21)
+    gx = rng.normal(size=(sc.n, 3)).astype(np.float32)
+    gv = rng.normal(size=(sc.n, 3)).astype(np.float32)
+    _, _, pT, vT, op, ov, par = _gpu_vjp(mps, sc, 4, 2, gx, gv)
+    R = A.RefScene(sc.pos4, sc.vel4, sc.bpos4, sc.material, sc.physics, False, K)
+    dx0, dv0, dmu, dsg, xT, _ = A.gradient(R, 4, gx.astype(np.float64), gv.astype(np.float64))
+    assert rel_norm(pT[:, :3], xT) < 1e-5
+    assert rel_norm(ov[:, :3], dv0) < 1e-3
+    assert rel_norm(op[:, :3], dx0) < 1e-3
+    assert abs(par[0, 0] - dmu) <= 1e-3 * abs(dmu)
+    assert abs(par[0, 1] - dsg) <= 1e-3 * abs(dsg)

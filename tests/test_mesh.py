@@ -69,3 +69,23 @@ def test_mesh_sampling_matches_reference(mps, tmp_path, n):
     assert np.all(np.diff(fid.astype(np.int64)) >= 0)  # written face by face
     # every sample lies on the box surface
     assert np.abs(np.abs(ours[:, :3]).max(1) - 4.5).max() < 1e-5
+
+
+@pytest.mark.gpu
+def test_step_with_mesh_sampled_boundary(mps, orc, tmp_path):
+    """A fluid block inside a box whose boundary particles come from mesh sampling: full steps
+    against the oracle (fixed iteration counts)."""
+    from mps_cuda_gb300 import Simulation, scenes
+    path = tmp_path / "box.obj"
+    write_box_obj(path, n=4)
+    V, F = scenes.load_obj(path, center=(0.25, 0.25, 0.25), size=(0.5, 0.5, 0.5))
+    sc = scenes.dam_break_small(8, seed=3)
+    sc.bpos4 = scenes.sample_mesh(V, F, 0.04)      # spacing 0.02, particle radius 0.01
+    sim = Simulation.from_scene(sc, fixed_iters=4)
+    o = orc.from_scene(sc, config=dict(fixed_iters=4))
+    sim.step(3)
+    o.step(3)
+    p, v = sim.get_fluid()
+    rp, rv = o.get("pos"), o.get("vel")
+    assert np.abs(p[:, :3] - rp).max() / np.abs(rp).max() < 1e-5
+    assert np.abs(v[:, :3] - rv).max() / np.abs(rv).max() < 1e-4
