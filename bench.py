@@ -420,10 +420,14 @@ def run_adjoint(args, rank, world, local_rank):
     from mps_cuda_gb300 import BatchedSimulation, build, scenes
     from mps_cuda_gb300.adjoint import AdjointRollout, com_loss, rollout
     build.build()
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl")
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
-    scs = scenes.adjoint_scenes(32, seed=rank)
+    scs = scenes.adjoint_scenes(32, seed=rank)   # every rank its own 32 scenes (weak scaling)
     horizon = args.steps
     every = 20
     K = int(scs[0].config["fixed_iters"])
@@ -451,6 +455,8 @@ def run_adjoint(args, rank, world, local_rank):
     roll = AdjointRollout(sim, horizon, every)
     roll.reserve()
     torch.cuda.synchronize(dev)
+    if dist:
+        td.barrier()
     e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
     with ClockSampler(local_rank) as clk:
         sim.set_fluid(p0, v0)
@@ -466,8 +472,12 @@ def run_adjoint(args, rank, world, local_rank):
         e3.synchronize()
     assert L_check == 0
     fwd_ms, bwd_ms = e0.elapsed_time(e1), e2.elapsed_time(e3)
+    if dist:   # the slowest rank's times; the value counts every rank's particles
+        t = torch.tensor([fwd_ms, bwd_ms], dtype=torch.float64, device=dev)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        fwd_ms, bwd_ms = float(t[0]), float(t[1])
     total_ms = fwd_ms + bwd_ms
-    value = n * horizon / (total_ms / 1e3)
+    value = n * world * horizon / (total_ms / 1e3)
     # e2e: the torch.autograd harness with host tensors (state H2D, rollout, D2H, loss, reverse)
     x0 = torch.tensor(p0[:, :3], dtype=torch.float64, requires_grad=True)
     v0t = torch.tensor(v0[:, :3], dtype=torch.float64, requires_grad=True)
@@ -479,6 +489,10 @@ def run_adjoint(args, rank, world, local_rank):
     com_loss(xT, vTt, mass, sim.offsets, targets).sum().backward()
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        e2e_s = float(t.item())
     same = bool(np.allclose(v0t.grad.numpy(), ov[:, :3], rtol=0, atol=0))
     line = {
         "metric": "particle-steps/s (DFSPH adjoint: forward + reverse, 32 x 16k scenes)", "value": value,
@@ -497,7 +511,7 @@ def run_adjoint(args, rank, world, local_rank):
                  "d_surface_tension_mean": float(par[:, 1].mean()), "finite": bool(np.isfinite(ov).all() and np.isfinite(par).all())},
         "roofline": None,
         "roofline_note": "per-kernel HBM roofline is reported by the plain-step line (dam_break_1m)",
-        "e2e": {"value": n * horizon / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (32 * n + 32 * n) / horizon,
+        "e2e": {"value": n * world * horizon / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (32 * n + 32 * n) / horizon,
                 "d2h_bytes_per_step": (32 * n + 32 * n + 32 * n) / horizon,
                 "note": "torch.autograd.Function over the C ABI: initial state in, final state out, cotangents in, "
                         "gradients out, host loss; bytes amortised over the horizon", "same_gradient": same},
@@ -510,6 +524,8 @@ def run_adjoint(args, rank, world, local_rank):
         line["gradient_check"] = [fd_check(scs[k], args.check_steps, min(every, args.check_steps), local_rank)
                                   for k in range(args.check_scenes)]
     sim.close()
+    if dist:
+        td.destroy_process_group()
     return line
 
 
