@@ -11,7 +11,8 @@
 //   - mps::System: SetDevice, OnUpdate (one frame of MPSSystem.cpp:191-291, skipped while the
 //     simulation is paused as b_runSim does), the frame counter; the scene set-up that the
 //     reference hard-codes in Initalize / *TestScene is passed in (SetPhysics, SetMaterial,
-//     SetFluid, SetBoundary, SampleBoundaryMesh).
+//     SetFluid, SetBoundary, SampleBoundaryMesh);
+//   - mps::kernel::*: the frame's phases under the names of the functions OnUpdate calls.
 // Differences: errors throw mps::Error (the reference reports nothing); state lives in the
 // library and is read back with GetFluid / GetField instead of GL-mapped buffers.
 #pragma once
@@ -234,6 +235,12 @@ public:
         return s;
     }
     mps_handle* Handle() const { return m_h; }
+    // One sub-phase of the frame (MPS_PHASE_SORT ... MPS_PHASE_ADVECT, in order); the last one
+    // completes the frame.
+    void Phase(int32_t phase, void* stream = nullptr) {
+        Check(mps_phase(m_h, phase, stream));
+        if (phase == MPS_PHASE_ADVECT) m_frame++;
+    }
 
 private:
     mps_handle* m_h = nullptr;
@@ -244,5 +251,39 @@ private:
     bool b_runSim = true;
     uint64_t m_frame = 0;
 };
+
+// The frame's phases under the names of the reference's functions that OnUpdate calls
+// (MPSSystem.cpp:220-278), so that its call sequence can be kept.  Each runs on all of the
+// System's particles; several reference calls map to one phase, as noted.
+namespace kernel {
+// SpatialHash::UpdateHash + ZSort (MPSSpatialHash.cu:53-140): cell keys, sort, reorder.
+inline void UpdateHash(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_SORT, stream); }
+// SpatialHash::BuildNeighorhood, fluid-fluid and fluid-boundary (MPSSpatialHash.cu:142-218).
+inline void BuildNeighorhood(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_NEIGHBORS, stream); }
+namespace SPH {
+// ComputeBoundaryParticleVolumeSub/Final (MPSSPHBaseUtil.cu:9-53); a no-op unless the config
+// asks for the reference's accumulating volume (the static boundary's volume is set once).
+inline void ComputeBoundaryParticleVolume(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_BVOLUME, stream); }
+// ComputeDensitySub/Final + DensityColorTest + ComputeDFSPHFactorSub/Final, then ResetForce /
+// ApplyGravity / UpdateVelocity (MPSSystem.cpp:240-255): one fused pass.
+inline void ComputeDensityAndDFSPHFactor(System& sys, void* stream = nullptr) {
+    sys.Phase(MPS_PHASE_DENSITY_ALPHA, stream);
+}
+// ComputeDFSPHDivergenceFree (MPSSPHDFSPHUtil.h:80-87).
+inline void ComputeDFSPHDivergenceFree(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_DF, stream); }
+// ApplyImplicitViscosityNSurfaceTension (MPSSPHNonPressureUtil.h:61-65).
+inline void ApplyImplicitViscosityNSurfaceTension(System& sys, void* stream = nullptr) {
+    sys.Phase(MPS_PHASE_VISCST, stream);
+}
+// ComputeDFSPHConstantDensity (MPSSPHDFSPHUtil.h:72-79).
+inline void ComputeDFSPHConstantDensity(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_CD, stream); }
+}  // namespace SPH
+namespace Advect {
+// BoundaryCollision + UpdatePosition (MPSAdvectUtil.h:17-19); completes the frame.
+inline void BoundaryCollisionAndUpdatePosition(System& sys, void* stream = nullptr) {
+    sys.Phase(MPS_PHASE_ADVECT, stream);
+}
+}  // namespace Advect
+}  // namespace kernel
 
 }  // namespace mps

@@ -1,7 +1,10 @@
 // The small dam break (10^3 fluid particles, r = 0.01, spacing 0.02, walls of a 0.5 m box) driven
 // through the C++ layer the way mps::System drives the reference's step; writes the final fluid
-// state (pos4 then vel4, float32, particle-ID order) to argv[1].
+// state (pos4 then vel4, float32, particle-ID order) to argv[1]; argv[3] = "phases" runs each frame
+// through the mps::kernel phase functions in the reference's OnUpdate order instead of OnUpdate.
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "mps_system.hpp"
@@ -54,7 +57,22 @@ int main(int argc, char** argv) {
         mps::Check(mps_gen_block(10, 10, 10, lo, spacing, r, mat.GetMass(), 0.002, 0, p4.data(), v4.data()));
         sys.SetFluid(p4, v4);
 
-        for (int f = 0; f < frames; ++f) sys.OnUpdate();
+        const bool phases = argc > 3 && std::string(argv[3]) == "phases";
+        for (int f = 0; f < frames; ++f) {
+            if (!phases) {
+                sys.OnUpdate();
+                continue;
+            }
+            // the reference's OnUpdate call sequence (MPSSystem.cpp:220-278), phase by phase
+            mps::kernel::UpdateHash(sys);
+            mps::kernel::BuildNeighorhood(sys);
+            mps::kernel::SPH::ComputeBoundaryParticleVolume(sys);
+            mps::kernel::SPH::ComputeDensityAndDFSPHFactor(sys);
+            mps::kernel::SPH::ComputeDFSPHDivergenceFree(sys);
+            mps::kernel::SPH::ApplyImplicitViscosityNSurfaceTension(sys);
+            mps::kernel::SPH::ComputeDFSPHConstantDensity(sys);
+            mps::kernel::Advect::BoundaryCollisionAndUpdatePosition(sys);
+        }
         sys.SetRunning(false);
         sys.OnUpdate();   // paused: no step
         std::vector<float> pos, vel;

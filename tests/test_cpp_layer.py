@@ -57,3 +57,10 @@ def test_cpp_example_matches_python_api(mps, tmp_path):
     sim.step(20)
     p, v = sim.get_fluid()
     assert np.array_equal(data[0], p) and np.array_equal(data[1], v)
+    # the same frames through the phase functions (the reference's OnUpdate call sequence)
+    out2 = tmp_path / "state_phases.bin"
+    r = subprocess.run([str(exe), str(out2), "20", "phases"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "frames 20 steps 20" in r.stdout
+    data2 = np.fromfile(out2, np.float32).reshape(2, -1, 4)
+    assert np.array_equal(data2, data)
