@@ -20,6 +20,8 @@ BUILD = HERE / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
+# Extra nvcc flags (e.g. -DMPSG_B_AP=8 to retune a neighbour loop); a change needs build(force=True).
+NVCC_FLAGS += os.environ.get("MPS_GB300_NVCC_FLAGS", "").split()
 SOURCES = ["sort.cu", "sph.cu", "api.cu", "noalloc.cu", "mesh.cu", "adjoint.cu", "scene.cpp"]
 
 

@@ -206,33 +206,105 @@ struct Kahan {
 // the batch's indices and the per-pair data streamed in the same layout (stream(k)), phase 2
 // issues every gather (gather(j, k)), phase 3 runs use(gathered, streamed, k) in k order.  A
 // thread so keeps B index + stream loads, then B gathers, in flight, and sums in the same order as
-// a plain loop (results are bit-identical for every B).
+// a plain loop (results are bit-identical for every B and PF).  PF != 0 pipelines the loop: the next
+// batch's indices and streamed data load while this batch's gathers are in flight.
 struct NoStream {};
-template <int B, class S, class T, class Stream, class Gather, class Use>
+
+// Loads of the per-pair streams (neighbour indices, CG coefficients).  Each item is read once per
+// pass, so the loads skip L1 allocation (L1::no_allocate) and leave L1 to the neighbour gathers,
+// which the warp's other lanes reuse.  MPSG_STREAM_HINT=0 restores plain loads.
+#ifndef MPSG_STREAM_HINT
+#define MPSG_STREAM_HINT 1
+#endif
+__device__ __forceinline__ unsigned ld_stream(const unsigned* p) {
+#if MPSG_STREAM_HINT
+    unsigned v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+#else
+    return *p;
+#endif
+}
+__device__ __forceinline__ float2 ld_stream(const float2* p) {
+#if MPSG_STREAM_HINT
+    float2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+    return v;
+#else
+    return *p;
+#endif
+}
+template <int B, class S, class T, int PF = 0, class Stream, class Gather, class Use>
 __device__ __forceinline__ void visit_batched(const unsigned* __restrict__ list, size_t stride, int i, int n,
                                               Stream stream, Gather gather, Use use) {
     int k = 0;
-    for (; k + B <= n; k += B) {
+    if constexpr (PF != 0) {
         unsigned jj[B];
         S ss[B];
+        if (n >= B) {
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
-            jj[u] = list[size_t(k + u) * stride + size_t(i)];
-            ss[u] = stream(k + u);
+            for (int u = 0; u < B; ++u) {
+                jj[u] = ld_stream(list + size_t(u) * stride + size_t(i));
+                ss[u] = stream(u);
+            }
         }
-        T v[B];
+        for (; k + B <= n; k += B) {
+            T v[B];
+            S sc[B];
 #pragma unroll
-        for (int u = 0; u < B; ++u) v[u] = gather(jj[u], k + u);
+            for (int u = 0; u < B; ++u) {
+                v[u] = gather(jj[u], k + u);
+                sc[u] = ss[u];
+            }
+            if (k + 2 * B <= n) {
 #pragma unroll
-        for (int u = 0; u < B; ++u) use(v[u], ss[u], k + u);
+                for (int u = 0; u < B; ++u) {
+                    jj[u] = ld_stream(list + size_t(k + B + u) * stride + size_t(i));
+                    ss[u] = stream(k + B + u);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < B; ++u) use(v[u], sc[u], k + u);
+        }
+    } else {
+        for (; k + B <= n; k += B) {
+            unsigned jj[B];
+            S ss[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                jj[u] = ld_stream(list + size_t(k + u) * stride + size_t(i));
+                ss[u] = stream(k + u);
+            }
+            T v[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) v[u] = gather(jj[u], k + u);
+#pragma unroll
+            for (int u = 0; u < B; ++u) use(v[u], ss[u], k + u);
+        }
     }
     for (; k < n; ++k) {
         const S sk = stream(k);
-        use(gather(list[size_t(k) * stride + size_t(i)], k), sk, k);
+        use(gather(ld_stream(list + size_t(k) * stride + size_t(i)), k), sk, k);
     }
 }
 
 // Batch sizes per loop (template arguments of visit_batched), set from GB300 sweeps.
+// Software-pipelined index loads per loop (PF of visit_batched), set from the same sweeps.
+#ifndef MPSG_PF_AP
+#define MPSG_PF_AP 0
+#endif
+#ifndef MPSG_PF_PA
+#define MPSG_PF_PA 1
+#endif
+#ifndef MPSG_PF_PB
+#define MPSG_PF_PB 0
+#endif
+#ifndef MPSG_PF_DENS
+#define MPSG_PF_DENS 0
+#endif
+#ifndef MPSG_PF_SETUP
+#define MPSG_PF_SETUP 0
+#endif
 #ifndef MPSG_B_AP
 #define MPSG_B_AP 4      // CG / Jacobi operator
 #endif

@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     Kahan rf, gx, gy, gz, sq;
     rf.add(p.V * kW(0.0f, invh, p.cubic));
-    visit_batched<MPSG_B_DENS, NoStream, float4>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; }, [&](unsigned j, int) { return d.pos[j]; },
+    visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; }, [&](unsigned j, int) { return d.pos[j]; },
                           [&](const float4& xj, NoStream, int) {
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         const float d2 = dx * dx + dy * dy + dz * dz;
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
         sq.add(ax * ax + ay * ay + az * az);
     });
     Kahan rb;
-    visit_batched<MPSG_B_DENS, NoStream, float4>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+    visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
                           [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
                           [&](const float4& xj, NoStream, int) {
         const float vb = xj.w;
@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         const unsigned c = d.cnt[i];
         const int nf = int(c & 0xffffu), nb = int(c >> 16);
         float df = 0.0f;
-        visit_batched<MPSG_B_PA, NoStream, XV>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+        visit_batched<MPSG_B_PA, NoStream, XV, MPSG_PF_PA>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
                           [&](unsigned j, int) { return XV{d.pos[j], d.vel[j]}; },
                           [&](const XV& t, NoStream, int) {
             const float4 xj = t.x, vj = t.v;
@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
             df += g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
         });
         float db = 0.0f;
-        visit_batched<MPSG_B_PA, NoStream, float4>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+        visit_batched<MPSG_B_PA, NoStream, float4, MPSG_PF_PA>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
                               [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
                               [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
             fx -= g * dx; fy -= g * dy; fz -= g * dz;
         }
     } else {
-        visit_batched<MPSG_B_PB, NoStream, float4>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+        visit_batched<MPSG_B_PB, NoStream, float4, MPSG_PF_PB>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
                               [&](unsigned j, int) { float4 x = d.pos[j]; x.w = d.kappa[j]; return x; },
                               [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
     fx *= 0.5f * p.V; fy *= 0.5f * p.V; fz *= 0.5f * p.V;
     if (ki != 0.0f) {
         float bx = 0.0f, by = 0.0f, bz = 0.0f;
-        visit_batched<MPSG_B_PB, NoStream, float4>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+        visit_batched<MPSG_B_PB, NoStream, float4, MPSG_PF_PB>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
                               [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
                               [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(BS) k_st_factor(Dev d, Params p) {
     const float invh = 1.0f / xi.w;
     const int nf = int(d.cnt[i] & 0xffffu);
     float acc = 0.0f;
-    visit_batched<MPSG_B_SETUP, NoStream, XV>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+    visit_batched<MPSG_B_SETUP, NoStream, XV, MPSG_PF_SETUP>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
                       [&](unsigned j, int) { return XV{d.pos[j], d.vel[j]}; },
                       [&](const XV& t, NoStream, int) {
         const float4 xj = t.x, vj = t.v;
@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
     float bx = 0.0f, by = 0.0f, bz = 0.0f;
     float csum = 0.0f, sxx = 0.0f, syy = 0.0f, szz = 0.0f, sxy = 0.0f, sxz = 0.0f, syz = 0.0f;  // Jacobi block sums
     float ax = 0.0f, ay = 0.0f, az = 0.0f;   // sum of the operator's pair terms applied to x0 = v
-    visit_batched<MPSG_B_SETUP, NoStream, XVA>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+    visit_batched<MPSG_B_SETUP, NoStream, XVA, MPSG_PF_SETUP>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
                        [&](unsigned j, int) { return XVA{d.pos[j], d.vel[j], d.aux[j]}; },
                        [&](const XVA& t, NoStream, int k) {
         const float4 xj = t.x, vj = t.v;
@@ -776,8 +776,8 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
     const float4 qi = q[i];
     const int nf = int(d.cnt[i] & 0xffffu);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    visit_batched<MPSG_B_AP, float2, XQ>(d.nbr_f, stride, i, nf,
-                       [&](int k) { return d.cg_coef[size_t(k) * stride + size_t(i)]; },
+    visit_batched<MPSG_B_AP, float2, XQ, MPSG_PF_AP>(d.nbr_f, stride, i, nf,
+                       [&](int k) { return ld_stream(d.cg_coef + size_t(k) * stride + size_t(i)); },
                        [&](unsigned j, int) { return XQ{d.pos[j], q[j]}; },
                        [&](const XQ& g, const float2& cf, int) {
         const float4 xj = g.x, qj = g.q;
