@@ -43,7 +43,12 @@ BOUNDARY_BYTES = 16
 
 def overrides(args) -> dict:
     """Library config fields set on the command line."""
-    return {} if args.cg_form is None else {"cg_form": args.cg_form}
+    out = {}
+    if args.cg_form is not None:
+        out["cg_form"] = args.cg_form
+    if args.block_size is not None:
+        out["block_size"] = args.block_size
+    return out
 
 
 def env_rank():
@@ -105,7 +110,8 @@ class ClockSampler:
 
 def radix_passes(sim) -> int:
     g = sim.grid()
-    cells = g["dims"][0] * g["dims"][1] * g["dims"][2]
+    nx, ny, nz = g["dims"]
+    cells = nx * (ny + ny % 2) * (nz + nz % 2)  # key space: ny, nz padded to whole 2 x 2 columns
     bits = max(1, math.ceil(math.log2(max(2, cells))))
     return math.ceil(bits / 8)
 
@@ -725,6 +731,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="precision_4m: block size scale (1 = 2 x 2M)")
     ap.add_argument("--cg-form", type=int, default=None, choices=[0, 1],
                     help="CG arrangement: 0 three-pass (the reference's, library default), 1 two-pass")
+    ap.add_argument("--block-size", type=int, default=None, choices=[64, 128, 256],
+                    help="threads per block of the neighbour-sum kernels (library default 128)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.steps is None:

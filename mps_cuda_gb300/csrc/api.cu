@@ -77,7 +77,7 @@ void mps_handle::release() {
     mpsg::host::adjoint_release(this);
     void** ptrs[] = {(void**)&pos[0], (void**)&pos[1], (void**)&vel[0], (void**)&vel[1], (void**)&ids[0],
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
-                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&nbr_l, (void**)&stage, (void**)&rho, (void**)&rdev,
+                     (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&rho, (void**)&rdev,
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol,
@@ -159,9 +159,6 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.nbr_f = h->nbr_f;
     d.nbr_b = h->nbr_b;
     d.cnt = h->cnt;
-    d.nbr_l = h->nbr_l;
-    d.stage = h->stage;
-    d.stage_on = h->cfg.stage ? 1 : 0;
     d.rho = h->rho;
     d.alpha = h->alpha;
     d.kappa = h->kappa;
@@ -226,7 +223,7 @@ int build_layout(mps_handle* h, const std::vector<float>& max_h_scene) {
         sc.ny = dims[1];
         sc.nz = dims[2];
         sc.key_base = key;
-        const unsigned long long cells = (unsigned long long)dims[0] * dims[1] * dims[2];
+        const unsigned long long cells = cell_key_count(dims[0], dims[1], dims[2]);
         key += cells;
         sc.bminx = float(lo[0]); sc.bminy = float(lo[1]); sc.bminz = float(lo[2]);
         sc.bmaxx = float(hi[0]); sc.bmaxy = float(hi[1]); sc.bmaxz = float(hi[2]);
@@ -280,8 +277,6 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->nbr_b, S * size_t(h->cfg.max_boundary_neighbors)));
     MPS_CUDA_TRY(dalloc(&h->cg_coef, S * size_t(h->cfg.max_fluid_neighbors)));
     MPS_CUDA_TRY(dalloc(&h->cnt, S));
-    MPS_CUDA_TRY(dalloc(&h->nbr_l, S * size_t(h->cfg.max_fluid_neighbors)));
-    MPS_CUDA_TRY(dalloc(&h->stage, S / 64 + 1));
     MPS_CUDA_TRY(cudaMemset(h->cnt, 0, S * sizeof(unsigned)));
     MPS_CUDA_TRY(dalloc(&h->rho, S));
     MPS_CUDA_TRY(dalloc(&h->alpha, S));
@@ -335,7 +330,7 @@ int upload_boundary(mps_handle* h) {
             const int cx = host_cell(x.x, sc.ox, sc.inv_cell, sc.nx);
             const int cy = host_cell(x.y, sc.oy, sc.inv_cell, sc.ny);
             const int cz = host_cell(x.z, sc.oz, sc.inv_cell, sc.nz);
-            key[size_t(b)] = sc.key_base + ((unsigned long long)cz * unsigned(sc.ny) + unsigned(cy)) * unsigned(sc.nx) + unsigned(cx);
+            key[size_t(b)] = cell_key(sc, cx, cy, cz);
         }
     }
     std::iota(ord.begin(), ord.end(), 0u);
@@ -770,6 +765,7 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;
     if (h->cfg.visc_solver != MPS_VISC_JACOBI) h->cfg.visc_solver = MPS_VISC_CG;
     if (h->cfg.cg_form != MPS_CG_TWO_PASS) h->cfg.cg_form = MPS_CG_THREE_PASS;
+    h->cfg.stage = 0;  // reserved
     *out = h;
     return MPS_OK;
 }

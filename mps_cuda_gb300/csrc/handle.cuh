@@ -46,8 +46,6 @@ struct mps_handle {
     unsigned* nbr_f = nullptr;
     unsigned* nbr_b = nullptr;
     unsigned* cnt = nullptr;
-    unsigned short* nbr_l = nullptr;
-    mpsg::Stage* stage = nullptr;
     float *rho = nullptr, *rdev = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
     float2* aux = nullptr;
     float4* color = nullptr;

@@ -33,15 +33,26 @@ struct Scene {
     int bbegin, bend;               // boundary particles of this scene (sorted order)
 };
 
-// Shared-memory staging of a thread block's fluid neighbourhood.  The block's particles occupy
-// cells [kf, kl] (key order); every fluid neighbour lies in one of the nine key ranges
-// [kf + off - 1, kl + off + 1], off = dz*nx*ny + dy*nx for dz, dy in {-1, 0, 1}.  Those map to
-// nine slot ranges, merged here into disjoint sorted ranges lo[r]..hi[r] that are staged back to
-// back from base[r]; base[9] is the staged count.  Neighbour lists also carry the local index.
-constexpr int kStageCap = 2048;     // records per block (above this the block gathers from global)
-struct Stage {
-    int lo[9], hi[9], base[10];
-};
+// Cell keys.  Cells are grouped in columns of kBrick x kBrick rows (y, z) that run along x; a
+// column's keys run over x, and for each x over its kBrick x kBrick rows (y fastest).  A run of
+// consecutive slots so covers a compact box of cells (a 128-slot block: about 4 x 2 x 2 cells at
+// 8 particles a cell) instead of a 16-cell stretch of one row, which shrinks the neighbourhood a
+// thread block gathers from from about 10x to about 6x its own cells.  grid_key is the key inside
+// one grid (ny and nz padded to whole columns); cell_key adds the scene's key base.
+constexpr unsigned kBrick = 2;
+__host__ __device__ __forceinline__ unsigned long long grid_key(int nx, int ny, int cx, int cy, int cz) {
+    const unsigned nyb = (unsigned(ny) + kBrick - 1) / kBrick;
+    const unsigned long long col = (unsigned long long)(unsigned(cz) / kBrick) * nyb + unsigned(cy) / kBrick;
+    return ((col * unsigned(nx) + unsigned(cx)) * kBrick + unsigned(cz) % kBrick) * kBrick + unsigned(cy) % kBrick;
+}
+__host__ __device__ __forceinline__ unsigned long long cell_key(const Scene& sc, int cx, int cy, int cz) {
+    return sc.key_base + grid_key(sc.nx, sc.ny, cx, cy, cz);
+}
+// Keys of an nx x ny x nz grid.
+__host__ __device__ __forceinline__ unsigned long long cell_key_count(int nx, int ny, int nz) {
+    const unsigned long long B = kBrick;
+    return (unsigned long long)nx * ((unsigned long long)(ny + B - 1) / B * B) * ((unsigned long long)(nz + B - 1) / B * B);
+}
 
 // Device-resident solver state of one scene.
 struct SceneSolve {
@@ -98,9 +109,6 @@ struct Dev {
     unsigned int* nbr_f;
     unsigned int* nbr_b;
     unsigned int* cnt;            // nf | nb << 16
-    unsigned short* nbr_l;        // block-local staged index of each fluid neighbour (like nbr_f)
-    Stage* stage;                 // staging layout per thread block of the pass kernels
-    int stage_on;                 // 1: pass kernels stage neighbour data in shared memory
     float* rho;
     float* rdev;                  // rho / rho0 - 1 from the compensated sums (the stiffness reads this)
     float* alpha;

@@ -47,7 +47,7 @@ __global__ void k_noalloc_keys(const float4* __restrict__ pos4, int n, float ox,
     const int cx = cell_coord(x.x, ox, inv, nx);
     const int cy = cell_coord(x.y, oy, inv, ny);
     const int cz = cell_coord(x.z, oz, inv, nz);
-    keys[i] = (static_cast<unsigned long long>(cz) * unsigned(ny) + unsigned(cy)) * unsigned(nx) + unsigned(cx);
+    keys[i] = grid_key(nx, ny, cx, cy, cz);
     vals[i] = unsigned(i);
 }
 
@@ -61,7 +61,7 @@ extern "C" int mps_cell_sort_noalloc(const float* pos4, int64_t n, const float o
     if (n < 0 || n > kMax) return MPS_E_INVALID;  // beyond the fixed scratch: rejected
     if (!origin || !dims || !(cell > 0.0f) || (n > 0 && (!pos4 || !keys_out || !order_out))) return MPS_E_INVALID;
     if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return MPS_E_INVALID;
-    const unsigned long long cells = (unsigned long long)dims[0] * dims[1] * dims[2];
+    const unsigned long long cells = cell_key_count(dims[0], dims[1], dims[2]);
     if (cells > (1ull << 40)) return MPS_E_INVALID;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPS_E_CUDA;

@@ -137,7 +137,7 @@ __global__ void k_keys(Dev d, Params p) {
     const int cy = cell_coord(x.y, sc.oy, sc.inv_cell, sc.ny);
     const int cz = cell_coord(x.z, sc.oz, sc.inv_cell, sc.nz);
     const int k = sc.coff + (slot - sc.slot_begin);
-    d.keys[k] = sc.key_base + (static_cast<unsigned long long>(cz) * unsigned(sc.ny) + unsigned(cy)) * unsigned(sc.nx) + unsigned(cx);
+    d.keys[k] = cell_key(sc, cx, cy, cz);
     d.vals[k] = unsigned(slot);
 }
 
@@ -182,94 +182,14 @@ __device__ __forceinline__ bool fluid_cell(const Dev& d, int slots, unsigned lon
     return e.x < e.y && e.x < unsigned(slots) && d.slot_key[e.x] == key;
 }
 
-// ------------------------------------------------------------------ shared-memory staging
-__device__ __forceinline__ int lower_bound_key(const unsigned long long* k, int a, int b, unsigned long long key) {
-    while (a < b) {
-        const int m = (a + b) >> 1;
-        if (k[m] < key) a = m + 1; else b = m;
-    }
-    return a;
-}
-__device__ __forceinline__ int upper_bound_key(const unsigned long long* k, int a, int b, unsigned long long key) {
-    while (a < b) {
-        const int m = (a + b) >> 1;
-        if (k[m] <= key) a = m + 1; else b = m;
-    }
-    return a;
-}
-
-// Computes the staging layout of this block (all threads call; result in st).  The nine key
-// ranges increase with (dz, dy) because ny >= 3, so merging them in order gives disjoint
-// sorted slot ranges.
-template <int BS>
-__device__ void compute_stage(const Dev& d, const Scene& sc, Stage& st) {
-    const int first = blockIdx.x * BS;
-    const int last = min(first + BS, sc.slot_begin + sc.n) - 1;
-    if (threadIdx.x < 9) {
-        int lo = sc.slot_begin, hi = sc.slot_begin;
-        if (last >= first) {
-            const int dz = int(threadIdx.x) / 3 - 1, dy = int(threadIdx.x) % 3 - 1;
-            const long long off = (long long)dz * sc.nx * sc.ny + (long long)dy * sc.nx;
-            const long long kb = (long long)sc.key_base;
-            const long long ke = kb + (long long)sc.nx * sc.ny * sc.nz - 1;
-            const long long klo = max((long long)d.slot_key[first] + off - 1, kb);
-            const long long khi = min((long long)d.slot_key[last] + off + 1, ke);
-            if (klo <= khi) {
-                const int e = sc.slot_begin + sc.n;
-                lo = lower_bound_key(d.slot_key, sc.slot_begin, e, (unsigned long long)klo);
-                hi = upper_bound_key(d.slot_key, lo, e, (unsigned long long)khi);
-            }
-        }
-        st.lo[threadIdx.x] = lo;
-        st.hi[threadIdx.x] = hi;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int e = st.lo[0], base = 0;
-        for (int r = 0; r < 9; ++r) {
-            const int lo = max(st.lo[r], e);
-            const int hi = max(st.hi[r], lo);
-            st.lo[r] = lo;
-            st.hi[r] = hi;
-            st.base[r] = base;
-            base += hi - lo;
-            e = hi;
-        }
-        st.base[9] = base;
-    }
-    __syncthreads();
-}
-
-// Block-local staged index of slot j (or -1 when j is outside the staged ranges).
-__device__ __forceinline__ int stage_index(const Stage& st, unsigned j) {
-    int loc = -1;
-#pragma unroll
-    for (int r = 0; r < 9; ++r)
-        if (int(j) >= st.lo[r] && int(j) < st.hi[r]) loc = st.base[r] + (int(j) - st.lo[r]);
-    return loc;
-}
-
-// Copies this block's staging layout from global memory into shared memory.
-__device__ __forceinline__ void load_stage(const Dev& d, Stage& st) {
-    if (threadIdx.x < 28) reinterpret_cast<int*>(&st)[threadIdx.x] = reinterpret_cast<const int*>(&d.stage[blockIdx.x])[threadIdx.x];
-    __syncthreads();
-}
-
 // ------------------------------------------------------------------ neighbour lists
 template <int BS>
 __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
     const Scene& sc = d.scenes[block_scene(d, BS)];
     __shared__ unsigned long long s_pf, s_pb;
-    __shared__ Stage st;
-    __shared__ int s_unmapped;
-    if (threadIdx.x == 0) { s_pf = 0; s_pb = 0; s_unmapped = 0; }
-    if (d.stage_on) {
-        compute_stage<BS>(d, sc, st);
-    } else {
-        __syncthreads();
-    }
-    const bool staged = d.stage_on && st.base[9] <= kStageCap;
+    if (threadIdx.x == 0) { s_pf = 0; s_pb = 0; }
+    __syncthreads();
     unsigned nf = 0, nb = 0;
     if (i < sc.slot_begin + sc.n) {
         const float4 xi = d.pos[i];
@@ -279,50 +199,38 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
         const int x0 = max(cx - 1, 0), x1 = min(cx + 1, sc.nx - 1);
         const size_t stride = size_t(p.slots);
         bool over = false;
+        // candidates cell by cell in (dz, dy, x) order, loaded kScan at a time (the loads do not
+        // depend on the tests, so a batch is in flight together)
+        auto fluid_test = [&](const float4& xj, unsigned j) {
+            if (j == unsigned(i)) return;
+            const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
+            const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
+            if (d2 < __fmul_rn(hij, hij)) {
+                if (nf < unsigned(p.cap_f)) d.nbr_f[size_t(nf) * stride + size_t(i)] = j; else over = true;
+                nf++;
+            }
+        };
+        auto bnd_test = [&](const float4& xj, unsigned j) {
+            const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
+            const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
+            if (d2 < __fmul_rn(hij, hij)) {
+                if (nb < unsigned(p.cap_b)) d.nbr_b[size_t(nb) * stride + size_t(i)] = j; else over = true;
+                nb++;
+            }
+        };
         for (int dz = -1; dz <= 1; ++dz) {
             const int z = cz + dz;
             if (z < 0 || z >= sc.nz) continue;
             for (int dy = -1; dy <= 1; ++dy) {
                 const int y = cy + dy;
                 if (y < 0 || y >= sc.ny) continue;
-                const unsigned long long row = sc.key_base + (static_cast<unsigned long long>(z) * unsigned(sc.ny) + unsigned(y)) * unsigned(sc.nx);
-                unsigned fb = 0xffffffffu, fe = 0u, bb = 0xffffffffu, be = 0u;
                 for (int x = x0; x <= x1; ++x) {
+                    const unsigned long long key = cell_key(sc, x, y, z);
                     uint2 e;
-                    if (fluid_cell(d, p.slots, row + unsigned(x), e)) { fb = min(fb, e.x); fe = max(fe, e.y); }
-                    const uint2 eb = d.btable[row + unsigned(x)];
-                    if (eb.x < eb.y) { bb = min(bb, eb.x); be = max(be, eb.y); }
+                    if (fluid_cell(d, p.slots, key, e)) scan_range(d.pos, e.x, e.y, fluid_test);
+                    const uint2 eb = d.btable[key];
+                    if (eb.x < eb.y) scan_range(d.bpos, eb.x, eb.y, bnd_test);
                 }
-                // candidates of a row range in order, loaded kScan at a time (the loads do not
-                // depend on the tests, so a batch is in flight together)
-                auto fluid_test = [&](const float4& xj, unsigned j) {
-                    if (j == unsigned(i)) return;
-                    const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
-                    const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
-                    if (d2 < __fmul_rn(hij, hij)) {
-                        if (nf < unsigned(p.cap_f)) {
-                            d.nbr_f[size_t(nf) * stride + size_t(i)] = j;
-                            if (staged) {
-                                const int loc = stage_index(st, j);
-                                if (loc < 0) s_unmapped = 1;
-                                d.nbr_l[size_t(nf) * stride + size_t(i)] = (unsigned short)(loc < 0 ? 0 : loc);
-                            }
-                        } else {
-                            over = true;
-                        }
-                        nf++;
-                    }
-                };
-                auto bnd_test = [&](const float4& xj, unsigned j) {
-                    const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
-                    const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
-                    if (d2 < __fmul_rn(hij, hij)) {
-                        if (nb < unsigned(p.cap_b)) d.nbr_b[size_t(nb) * stride + size_t(i)] = j; else over = true;
-                        nb++;
-                    }
-                };
-                scan_range(d.pos, fb, fe, fluid_test);
-                scan_range(d.bpos, bb, be, bnd_test);
             }
         }
         if (over) atomicOr(&d.ctr->flags, 1);
@@ -336,13 +244,6 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
     if (threadIdx.x == 0) {
         atomicAdd(&d.ctr->fluid_pairs, s_pf);
         atomicAdd(&d.ctr->boundary_pairs, s_pb);
-        // a block whose neighbours could not all be mapped (or that exceeds the capacity)
-        // gathers from global memory in the pass kernels
-        if (d.stage_on && (!staged || s_unmapped)) st.base[9] = kStageCap + 1;
-    }
-    if (d.stage_on) {
-        __syncthreads();
-        if (threadIdx.x < 28) reinterpret_cast<int*>(&d.stage[blockIdx.x])[threadIdx.x] = reinterpret_cast<const int*>(&st)[threadIdx.x];
     }
 }
 
@@ -367,7 +268,7 @@ __global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
     for (int z = max(cz - 1, 0); z <= min(cz + 1, sc.nz - 1); ++z)
         for (int y = max(cy - 1, 0); y <= min(cy + 1, sc.ny - 1); ++y)
             for (int x = max(cx - 1, 0); x <= min(cx + 1, sc.nx - 1); ++x) {
-                const uint2 e = d.btable[sc.key_base + (static_cast<unsigned long long>(z) * unsigned(sc.ny) + unsigned(y)) * unsigned(sc.nx) + unsigned(x)];
+                const uint2 e = d.btable[cell_key(sc, x, y, z)];
                 for (unsigned j = e.x; j < e.y; ++j) {
                     if (j == unsigned(b)) continue;
                     const float4 xj = d.bpos[j];
@@ -560,24 +461,6 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
     if (!profile && !d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
-    extern __shared__ float4 s_xk[];  // staged (x, y, z, kappa) of the block's neighbourhood
-    __shared__ Stage st;
-    bool staged = false;
-    if (d.stage_on) {
-        load_stage(d, st);
-        staged = st.base[9] <= kStageCap;
-        if (staged) {
-            for (int r = 0; r < 9; ++r) {
-                const int lo = st.lo[r], len = st.hi[r] - lo, b = st.base[r];
-                for (int t = threadIdx.x; t < len; t += BS) {
-                    float4 x = d.pos[lo + t];
-                    x.w = d.kappa[lo + t];
-                    s_xk[b + t] = x;
-                }
-            }
-            __syncthreads();
-        }
-    }
     if (i >= sc.slot_begin + sc.n) return;
     const size_t stride = size_t(p.slots);
     const float4 xi = d.pos[i];
@@ -586,26 +469,15 @@ __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile,
     const unsigned c = d.cnt[i];
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    if (staged) {
-        for (int k = 0; k < nf; ++k) {
-            const float4 xj = s_xk[d.nbr_l[size_t(k) * stride + size_t(i)]];
-            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            const float invd = safe_rsqrt(d2);
-            const float g = (ki + xj.w) * kG(d2 * invd, invd, invh, p.cubic);
-            fx -= g * dx; fy -= g * dy; fz -= g * dz;
-        }
-    } else {
-        visit_batched<MPSG_B_PB, NoStream, float4, MPSG_PF_PB>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
-                              [&](unsigned j, int) { float4 x = d.pos[j]; x.w = d.kappa[j]; return x; },
-                              [&](const float4& xj, NoStream, int) {
-            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            const float invd = safe_rsqrt(d2);
-            const float g = (ki + xj.w) * kG(d2 * invd, invd, invh, p.cubic);
-            fx -= g * dx; fy -= g * dy; fz -= g * dz;
-        });
-    }
+    visit_batched<MPSG_B_PB, NoStream, float4, MPSG_PF_PB>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
+                          [&](unsigned j, int) { float4 x = d.pos[j]; x.w = d.kappa[j]; return x; },
+                          [&](const float4& xj, NoStream, int) {
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float invd = safe_rsqrt(d2);
+        const float g = (ki + xj.w) * kG(d2 * invd, invd, invh, p.cubic);
+        fx -= g * dx; fy -= g * dy; fz -= g * dz;
+    });
     fx *= 0.5f * p.V; fy *= 0.5f * p.V; fz *= 0.5f * p.V;
     if (ki != 0.0f) {
         float bx = 0.0f, by = 0.0f, bz = 0.0f;
@@ -1109,13 +981,6 @@ int nblocks_for(int n, int bs) { return (n + bs - 1) / bs; }
         else if ((bs) == 64) KERNEL<64><<<p.slots / 64, 64, 0, s>>>(__VA_ARGS__);            \
         else KERNEL<256><<<p.slots / 256, 256, 0, s>>>(__VA_ARGS__);                         \
     } while (0)
-// Same with `smem` bytes of dynamic shared memory (the staged neighbourhood).
-#define MPSG_BS_SWITCH_SMEM(bs, smem, KERNEL, ...)                                           \
-    do {                                                                                     \
-        if ((bs) == 128) KERNEL<128><<<p.slots / 128, 128, (smem), s>>>(__VA_ARGS__);        \
-        else if ((bs) == 64) KERNEL<64><<<p.slots / 64, 64, (smem), s>>>(__VA_ARGS__);       \
-        else KERNEL<256><<<p.slots / 256, 256, (smem), s>>>(__VA_ARGS__);                    \
-    } while (0)
 
 void launch_keys(const Dev& d, const Params& p, cudaStream_t s) {
     k_keys<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
@@ -1144,10 +1009,10 @@ void launch_pressure_A(const Dev& d, const Params& p, int mode, int bs, unsigned
 }
 void launch_pressure_B(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                        cudaStream_t s) {
-    MPSG_BS_SWITCH_SMEM(bs, d.stage_on ? kStageCap * sizeof(float4) : 0, k_pressure_B, d, p, 0, cond, use_cond, limit);
+    MPSG_BS_SWITCH(bs, k_pressure_B, d, p, 0, cond, use_cond, limit);
 }
 void launch_pressure_B_profile(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-    MPSG_BS_SWITCH_SMEM(bs, d.stage_on ? kStageCap * sizeof(float4) : 0, k_pressure_B, d, p, 1, 0ull, 0, 0);
+    MPSG_BS_SWITCH(bs, k_pressure_B, d, p, 1, 0ull, 0, 0);
 }
 void launch_solver_finish(const Dev& d, const Params& p, int which, cudaStream_t s) {
     k_solver_finish<<<1, 256, 0, s>>>(d, p, which);

@@ -833,13 +833,22 @@ static inline int cell_coord(float x, float o, float inv, int dim) {
     return c < dim ? c : dim - 1;
 }
 
+// Key of cell (cx, cy, cz): cells grouped in columns of 2 x 2 rows (y, z) along x; inside a
+// column the key runs over x, then over the column's 4 rows (y fastest); ny and nz are padded to
+// even counts.  The GPU step's key layout (grid_key of the CUDA library), restated.
+static inline uint64_t new_key(const orc_grid* g, int cx, int cy, int cz) {
+    const uint64_t nyb = (uint64_t(g->dims[1]) + 1) / 2;
+    const uint64_t col = uint64_t(cz / 2) * nyb + uint64_t(cy / 2);
+    return g->key_base + ((col * uint64_t(g->dims[0]) + uint64_t(cx)) * 2 + uint64_t(cz % 2)) * 2 + uint64_t(cy % 2);
+}
+
 void orc_new_keys(int64_t n, const float* pos4, const orc_grid* g, uint64_t* keys) {
     for (int64_t i = 0; i < n; ++i) {
         const float* p = pos4 + 4 * i;
         const int cx = cell_coord(p[0], g->origin[0], g->inv_cell, g->dims[0]);
         const int cy = cell_coord(p[1], g->origin[1], g->inv_cell, g->dims[1]);
         const int cz = cell_coord(p[2], g->origin[2], g->inv_cell, g->dims[2]);
-        keys[i] = g->key_base + (uint64_t(cz) * uint64_t(g->dims[1]) + uint64_t(cy)) * uint64_t(g->dims[0]) + uint64_t(cx);
+        keys[i] = new_key(g, cx, cy, cz);
     }
 }
 
@@ -890,7 +899,7 @@ void orc_new_nbr_counts(int64_t nq, const float* q4, int64_t np, const float* p4
                 for (int dx = -1; dx <= 1; ++dx) {
                     const int x = cx + dx, y = cy + dy, z = cz + dz;
                     if (x < 0 || y < 0 || z < 0 || x >= g->dims[0] || y >= g->dims[1] || z >= g->dims[2]) continue;
-                    const uint64_t key = g->key_base + (uint64_t(z) * uint64_t(g->dims[1]) + uint64_t(y)) * uint64_t(g->dims[0]) + uint64_t(x);
+                    const uint64_t key = new_key(g, x, y, z);
                     uint32_t s, e;
                     find(key, s, e);
                     for (uint32_t j = s; j < e; ++j) {

@@ -112,7 +112,8 @@ typedef struct orc_grid {
     uint64_t key_base;   /* offset of this grid's cells in the global key space */
 } orc_grid;
 
-/* key = key_base + (cz*ny + cy)*nx + cx with clamped FP32 cell coordinates. */
+/* key = key_base + ((((cz/2)*ceil(ny/2) + cy/2)*nx + cx)*2 + cz%2)*2 + cy%2 with clamped FP32 cell
+ * coordinates (columns of 2 x 2 rows along x). */
 void orc_new_keys(int64_t n, const float* pos4, const orc_grid* g, uint64_t* keys);
 /* Stable sort of (key, value) pairs by key (LSD semantics: ties keep input order). */
 void orc_new_stable_sort(int64_t n, uint64_t* keys, uint32_t* vals);

@@ -159,19 +159,6 @@ def test_graph_step_equals_eager_phases(mps):
     assert a.stats() ["cd_iters"] == b.stats()["cd_iters"]
 
 
-def test_shared_memory_staging_is_bit_identical(mps):
-    """Staged neighbourhoods and global gathers read the same data in the same order."""
-    from mps_cuda_gb300 import Simulation, scenes
-    sc = scenes.dam_break_small(14, seed=12)
-    a = Simulation.from_scene(sc, stage=1)
-    b = Simulation.from_scene(sc, stage=0)
-    a.step(3)
-    b.step(3)
-    pa, va = a.get_fluid()
-    pb, vb = b.get_fluid()
-    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
-
-
 def test_deterministic(mps):
     from mps_cuda_gb300 import Simulation, scenes
     sc = scenes.dam_break_small(10, seed=4)

@@ -98,13 +98,17 @@ def test_new_scheme_keys_sort_ranges(orc):
     p4 = np.zeros((8, 4), np.float32)
     p4[:, :3] = pts
     keys = orc.new_keys(p4, g)
-    # key = (cz * ny + cy) * nx + cx with clamping; NaN -> cell 0 on that axis
-    expect = [0, (1 * 3 + 2) * 4 + 3, 1, 0, (0 * 3 + 2) * 4 + 0, 1, (1 * 3 + 0) * 4 + 3, 0]
+    # columns of 2 x 2 rows (y, z) along x: col = (cz // 2) * ceil(ny / 2) + cy // 2,
+    # key = ((col * nx + cx) * 2 + cz % 2) * 2 + cy % 2, with clamping; NaN -> cell 0 on that axis.
+    # cells: (0,0,0) (3,2,1) (1,0,0) (0,0,0) (0,2,0) (1,0,0) (3,0,1) (0,0,0); ceil(3 / 2) = 2
+    expect = [0, ((1 * 4 + 3) * 2 + 1) * 2 + 0, ((0 * 4 + 1) * 2 + 0) * 2 + 0, 0, ((1 * 4 + 0) * 2 + 0) * 2 + 0,
+              ((0 * 4 + 1) * 2 + 0) * 2 + 0, ((0 * 4 + 3) * 2 + 1) * 2 + 0, 0]
+    assert expect == [0, 30, 4, 0, 16, 4, 14, 0]
     assert keys.tolist() == expect
     sk, sv = orc.new_stable_sort(keys, np.arange(8, dtype=np.uint32))
-    assert sv.tolist() == [0, 3, 7, 2, 5, 4, 6, 1]  # ties keep input order
+    assert sv.tolist() == [0, 3, 7, 2, 5, 6, 4, 1]  # ties keep input order
     cells, st, en = orc.new_cell_ranges(sk)
-    assert cells.tolist() == [0, 1, 8, 15, 23]
+    assert cells.tolist() == [0, 4, 14, 16, 30]
     assert st.tolist() == [0, 3, 5, 6, 7]
     assert en.tolist() == [3, 5, 6, 7, 8]
 
