@@ -785,49 +785,95 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
     }
 }
 
+// The three-pass CG's vector passes cover kVecSlots slots per block with NT threads (kVecSlots / NT
+// slots a thread, their loads issued before any store), which keeps more independent loads in
+// flight per thread than one slot a thread.  Blocks keep the 256-slot scene chunks, so the
+// per-block partials and the last-block sum are laid out as for the neighbour kernels.
+constexpr int kVecSlots = 256;
+#ifndef MPSG_VEC_NT
+#define MPSG_VEC_NT 128
+#endif
+
+// Deterministic sum of this scene's per-block partials (component c of 2) for blocks of SPB slots,
+// run by one block of NT threads.
+template <int NT, int SPB>
+__device__ double scene_partial_sum_nt(const Dev& d, const Scene& sc, int c, double* sh) {
+    const int b0 = sc.slot_begin / SPB, b1 = sc.slot_end / SPB;
+    double v = 0.0;
+    for (int b = b0 + threadIdx.x; b < b1; b += NT) v += __ldcg(d.partial + 2 * b + c);
+    return block_sum<NT>(v, sh);
+}
+
 // x += alpha p, r -= alpha Ap, beta = (r.r)_new / (r.r)_old.
-template <int BS>
-__global__ void __launch_bounds__(BS) k_cg_update3(Dev d, Params p) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p) {
+    constexpr int U = kVecSlots / NT;
     __shared__ double sh[32];
-    __shared__ double2 sh2[BS / 32];
-    const int s = block_scene(d, BS);
+    __shared__ double2 sh2[NT / 32];
+    const int s = block_scene(d, kVecSlots);
     if (!d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
-    const int i = blockIdx.x * BS + threadIdx.x;
-    float rr = 0.0f;
-    if (i < sc.slot_begin + sc.n) {
-        const float a = float(d.solve[s].cg_alpha);
-        float4 x = d.cg_x[i];
-        float4 r = d.cg_r[i];
-        const float4 q = d.cg_p[i];
-        const float4 ap = d.cg_ap[i];
-        x.x += a * q.x; x.y += a * q.y; x.z += a * q.z;
-        r.x -= a * ap.x; r.y -= a * ap.y; r.z -= a * ap.z;
-        d.cg_x[i] = x;
-        d.cg_r[i] = r;
-        rr = r.x * r.x + r.y * r.y + r.z * r.z;
+    const int end = sc.slot_begin + sc.n;
+    const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
+    const float a = float(d.solve[s].cg_alpha);
+    float4 x[U], r[U], q[U], ap[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * NT;
+        if (i < end) {
+            x[u] = d.cg_x[i];
+            r[u] = d.cg_r[i];
+            q[u] = d.cg_p[i];
+            ap[u] = d.cg_ap[i];
+        }
     }
-    const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
+    float rr = 0.0f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * NT;
+        if (i < end) {
+            x[u].x += a * q[u].x; x[u].y += a * q[u].y; x[u].z += a * q[u].z;
+            r[u].x -= a * ap[u].x; r[u].y -= a * ap[u].y; r[u].z -= a * ap[u].z;
+            d.cg_x[i] = x[u];
+            d.cg_r[i] = r[u];
+            rr += r[u].x * r[u].x + r[u].y * r[u].y + r[u].z * r[u].z;
+        }
+    }
+    const double2 bs2 = block_sum2_f<NT>(rr, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
-    if (!last_block_of_scene<BS>(d, s, sc)) return;
-    const double t = scene_partial_sum<BS>(d, sc, 0, sh);
+    if (!last_block_of_scene<kVecSlots>(d, s, sc)) return;
+    const double t = scene_partial_sum_nt<NT, kVecSlots>(d, sc, 0, sh);
     if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
 }
 
 // p = r + beta p (MPSCGKernel.cuh:196-207); the loop guard of the WHILE body.
-template <int BS>
-__global__ void __launch_bounds__(BS) k_cg_dir3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_cg_dir3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+    constexpr int U = kVecSlots / NT;
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
-    const int s = block_scene(d, BS);
+    const int s = block_scene(d, kVecSlots);
     if (!d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
-    const int i = blockIdx.x * BS + threadIdx.x;
-    if (i >= sc.slot_begin + sc.n) return;
+    const int end = sc.slot_begin + sc.n;
+    const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
     const float b = float(d.solve[s].cg_beta);
-    const float4 r = d.cg_r[i];
-    float4 q = d.cg_p[i];
-    q.x = r.x + b * q.x; q.y = r.y + b * q.y; q.z = r.z + b * q.z;
-    d.cg_p[i] = q;
+    float4 r[U], q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * NT;
+        if (i < end) {
+            r[u] = d.cg_r[i];
+            q[u] = d.cg_p[i];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * NT;
+        if (i < end) {
+            q[u].x = r[u].x + b * q[u].x; q[u].y = r[u].y + b * q[u].y; q[u].z = r[u].z + b * q[u].z;
+            d.cg_p[i] = q[u];
+        }
+    }
 }
 
 // One block-Jacobi sweep: r = b + f x0 - (A_0 + f I) q, q' = q + D^-1 r (D: the particle's 3x3
@@ -1039,12 +1085,12 @@ void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long con
 }
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     (void)bs;
-    MPSG_BS_SWITCH(256, k_cg_update3, d, p);
+    k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p);
 }
 void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s) {
     (void)bs;
-    MPSG_BS_SWITCH(256, k_cg_dir3, d, p, cond, use_cond, limit);
+    k_cg_dir3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, cond, use_cond, limit);
 }
 void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    const float4* src, float4* dst, cudaStream_t s) {
