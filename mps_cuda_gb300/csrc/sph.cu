@@ -83,13 +83,15 @@ __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double
     return block_sum<BS>(v, sh);
 }
 
-// Returns true in every thread of the block that is the last of its scene to finish.
+// Returns true in every thread of the block that is the last of its scene to finish.  Callers
+// write the block's partials from thread 0 just before; the last block reads only those partials,
+// so only thread 0 fences (its partial write before its ticket).  A fence in every thread would
+// make each wait for its own data stores to become visible device-wide.
 template <int BS>
 __device__ bool last_block_of_scene(const Dev& d, int s, const Scene& sc) {
     __shared__ int am_last;
-    __threadfence();
-    __syncthreads();
     if (threadIdx.x == 0) {
+        __threadfence();
         const unsigned nblk = unsigned((sc.slot_end - sc.slot_begin) / BS);
         const unsigned t = atomicAdd(reinterpret_cast<unsigned*>(&d.solve[s].blocks_done), 1u);
         am_last = (t == nblk - 1u);
@@ -377,17 +379,19 @@ template <int BS>
 __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, unsigned long long cond, int use_cond) {
     __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    // the slot's own data loads before the scene and solver-state lookups (the grid covers exactly
+    // the allocated slots; padding slots have no neighbours)
+    const float4 xi = d.pos[i];
+    const float4 vi = d.vel[i];
+    const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
     const Scene& sc = d.scenes[s];
-    const int i = blockIdx.x * BS + threadIdx.x;
     float err = 0.0f;
     if (i < sc.slot_begin + sc.n) {
         const size_t stride = size_t(p.slots);
-        const float4 xi = d.pos[i];
-        const float4 vi = d.vel[i];
         const float invh = 1.0f / xi.w;
-        const unsigned c = d.cnt[i];
         const int nf = int(c & 0xffffu), nb = int(c >> 16);
         float df = 0.0f;
         visit_batched<MPSG_B_PA, NoStream, XV, MPSG_PF_PA>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
@@ -457,16 +461,17 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
 template <int BS>
 __global__ void __launch_bounds__(BS) k_pressure_B(Dev d, Params p, int profile, unsigned long long cond, int use_cond, int limit) {
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int i = blockIdx.x * BS + threadIdx.x;
+    // own data before the scene and solver-state lookups, as in k_pressure_A
+    const float4 xi = d.pos[i];
+    const float ki = d.kappa[i];
+    const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
     if (!profile && !d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
-    const int i = blockIdx.x * BS + threadIdx.x;
     if (i >= sc.slot_begin + sc.n) return;
     const size_t stride = size_t(p.slots);
-    const float4 xi = d.pos[i];
     const float invh = 1.0f / xi.w;
-    const float ki = d.kappa[i];
-    const unsigned c = d.cnt[i];
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     visit_batched<MPSG_B_PB, NoStream, float4, MPSG_PF_PB>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
@@ -642,11 +647,10 @@ __global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
 
 // (A q)_i = q_i (1 + f) + dt [sum_j c_ij (q_i - q_j) - sum_j cv_ij ((q_i - q_j).x_ij) x_ij]
 // with the coefficients of k_cg_b (MPSSPHNonPressureUtil.cuh:523-648).
-__device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, const float4* q, float factor) {
+__device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, const float4* q, float factor,
+                                          float4 xi, float4 qi, unsigned cnt) {
     const size_t stride = size_t(p.slots);
-    const float4 xi = d.pos[i];
-    const float4 qi = q[i];
-    const int nf = int(d.cnt[i] & 0xffffu);
+    const int nf = int(cnt & 0xffffu);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     visit_batched<MPSG_B_AP, float2, XQ, MPSG_PF_AP>(d.nbr_f, stride, i, nf,
                        [&](int k) { return ld_stream(d.cg_coef + size_t(k) * stride + size_t(i)); },
@@ -662,6 +666,9 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
     });
     const float f1 = 1.0f + factor;
     return make_float3(qi.x * f1 + p.dt * sx, qi.y * f1 + p.dt * sy, qi.z * f1 + p.dt * sz);
+}
+__device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, const float4* q, float factor) {
+    return apply_A(d, p, i, q, factor, d.pos[i], q[i], d.cnt[i]);
 }
 
 // Two-pass CG form (cg_form 1): the Chronopoulos-Gear arrangement (the same iterates as the
@@ -747,16 +754,19 @@ template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long long cond, int use_cond) {
     __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    // own data before the scene and solver-state lookups, as in k_pressure_A
+    const float4 xi = d.pos[i];
+    const float4 q = d.cg_p[i];
+    const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
     const Scene& sc = d.scenes[s];
-    const int i = blockIdx.x * BS + threadIdx.x;
     float rr = 0.0f, pap = 0.0f;
     if (i < sc.slot_begin + sc.n) {
-        const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor);
+        const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor, xi, q, c);
         d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
         const float4 r = d.cg_r[i];
-        const float4 q = d.cg_p[i];
         rr = r.x * r.x + r.y * r.y + r.z * r.z;
         pap = q.x * a.x + q.y * a.y + q.z * a.z;
     }
@@ -810,23 +820,23 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p) {
     constexpr int U = kVecSlots / NT;
     __shared__ double sh[32];
     __shared__ double2 sh2[NT / 32];
-    const int s = block_scene(d, kVecSlots);
-    if (!d.solve[s].do_update) return;
-    const Scene& sc = d.scenes[s];
-    const int end = sc.slot_begin + sc.n;
+    // the grid covers exactly the allocated slots, so the data loads go out before the scene and
+    // solver-state lookups (padding slots are loaded and not used)
     const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
-    const float a = float(d.solve[s].cg_alpha);
     float4 x[U], r[U], q[U], ap[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int i = i0 + u * NT;
-        if (i < end) {
-            x[u] = d.cg_x[i];
-            r[u] = d.cg_r[i];
-            q[u] = d.cg_p[i];
-            ap[u] = d.cg_ap[i];
-        }
+        x[u] = d.cg_x[i];
+        r[u] = d.cg_r[i];
+        q[u] = d.cg_p[i];
+        ap[u] = d.cg_ap[i];
     }
+    const int s = block_scene(d, kVecSlots);
+    if (!d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int end = sc.slot_begin + sc.n;
+    const float a = float(d.solve[s].cg_alpha);
     float rr = 0.0f;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -851,21 +861,18 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_cg_dir3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
     constexpr int U = kVecSlots / NT;
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
+    float4 r[U], q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {   // loads before the lookups, as in k_cg_update3
+        r[u] = d.cg_r[i0 + u * NT];
+        q[u] = d.cg_p[i0 + u * NT];
+    }
     const int s = block_scene(d, kVecSlots);
     if (!d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
     const int end = sc.slot_begin + sc.n;
-    const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
     const float b = float(d.solve[s].cg_beta);
-    float4 r[U], q[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int i = i0 + u * NT;
-        if (i < end) {
-            r[u] = d.cg_r[i];
-            q[u] = d.cg_p[i];
-        }
-    }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int i = i0 + u * NT;
