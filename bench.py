@@ -37,7 +37,7 @@ METRIC = "particle-steps/s (DFSPH, 1M fluid)"
 UNIT = "particle-steps/s"
 # algorithmic bytes per fluid particle of each kernel (compulsory SoA FP32 traffic) and per
 # boundary particle of a boundary-reading pass
-ALGO_BYTES = {"pressure_A": 44, "pressure_B": 52, "cg_ap": 72}
+ALGO_BYTES = {"pressure_A": 44, "pressure_B": 52, "cg_ap": 72, "cg_vector": 112}
 BOUNDARY_BYTES = 16
 
 
@@ -132,7 +132,7 @@ def cpu_baseline(scene, max_steps: int = 1):
 def run_ours(args, scene, rank, world, local_rank):
     import torch
     from mps_cuda_gb300 import Simulation, build
-    from mps_cuda_gb300._lib import K_CG_AP, K_PRESSURE_A, K_PRESSURE_B
+    from mps_cuda_gb300._lib import K_CG_AP, K_CG_VECTOR, K_PRESSURE_A, K_PRESSURE_B
 
     build.build()
     dist = world > 1
@@ -206,8 +206,11 @@ def run_ours(args, scene, rank, world, local_rank):
     t_ap = sim.profile_kernel(K_CG_AP, reps, stream)
     shares = {"pressure_A": t_a * (runs[0] + runs[2]), "pressure_B": t_b * (runs[0] + runs[2]), "cg_ap": t_ap * runs[1]}
     per = {"pressure_A": t_a, "pressure_B": t_b, "cg_ap": t_ap}
+    if not args.cg_form:  # three-pass CG (default): its update + direction passes
+        per["cg_vector"] = sim.profile_kernel(K_CG_VECTOR, reps, stream)
+        shares["cg_vector"] = per["cg_vector"] * runs[1]
     dom = max(shares, key=shares.get)
-    bnd = scene.nb if dom != "cg_ap" else 0
+    bnd = scene.nb if dom.startswith("pressure") else 0
     algo = ALGO_BYTES[dom] * scene.n + BOUNDARY_BYTES * bnd
     peak, src = measured_peaks()
     achieved = algo / (per[dom] / 1e3) / 1e9
@@ -233,7 +236,8 @@ def run_ours(args, scene, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": src, "traffic": traffic, "traffic_source": "profiles/dram_traffic.json (ncu capture at 512k particles scaled to 1M)" if traffic else None,
                      "algorithmic_bytes_per_launch": algo, "ms_per_launch": per[dom],
-                     "ms_per_launch_all": per},
+                     "ms_per_launch_all": per,
+                     "solver_loop_kernels_ms_per_step": sum(shares.values()) / args.steps},
         "step_roofline": {"algorithmic_bytes_per_step": step_algo,
                           "achieved_gbs": step_algo / (ms_max / args.steps / 1e3) / 1e9},
         "e2e": e2e,

@@ -188,7 +188,8 @@ enum mps_kernel_id {
     MPS_K_CG_AP = 2,          /* viscosity + surface tension + XSPH operator pass of a CG iteration */
     MPS_K_DENSITY_ALPHA = 3,  /* density, colour, alpha, gravity */
     MPS_K_BUILD_NBRS = 4,     /* neighbour lists */
-    MPS_K_SORT = 5            /* cell keys + radix sort + reorder */
+    MPS_K_SORT = 5,           /* cell keys + radix sort + reorder */
+    MPS_K_CG_VECTOR = 6       /* the three-pass CG's update + direction passes of a CG iteration */
 };
 /* Times `reps` back-to-back launches of one kernel of the step on the current state with CUDA
  * events recorded on `stream`; *ms = mean milliseconds per launch.  Solver passes run in their

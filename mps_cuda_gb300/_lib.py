@@ -25,7 +25,7 @@ ERRORS = {
 
 PHASE_SORT, PHASE_NEIGHBORS, PHASE_BVOLUME, PHASE_DENSITY_ALPHA, PHASE_DF, PHASE_VISCST, PHASE_CD, PHASE_ADVECT = range(8)
 KERNEL_POLY6_SPIKY, KERNEL_CUBIC_SPLINE = 0, 1
-K_PRESSURE_A, K_PRESSURE_B, K_CG_AP, K_DENSITY_ALPHA, K_BUILD_NBRS, K_SORT = range(6)
+K_PRESSURE_A, K_PRESSURE_B, K_CG_AP, K_DENSITY_ALPHA, K_BUILD_NBRS, K_SORT, K_CG_VECTOR = range(7)
 VISC_CG, VISC_JACOBI = 0, 1
 CG_THREE_PASS, CG_TWO_PASS = 0, 1
 

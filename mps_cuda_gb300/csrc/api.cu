@@ -1090,6 +1090,7 @@ int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream
             case MPS_K_CG_AP:
                 if (p.cg_form == 1) launch_cg_ap(d, p, bs, 0ull, 2, s); else launch_cg_ap3(d, p, bs, 0ull, 2, s);
                 break;
+            case MPS_K_CG_VECTOR: launch_cg_vector_profile(d, p, s); break;
             case MPS_K_DENSITY_ALPHA: launch_density_alpha(d, p, bs, s); break;
             case MPS_K_BUILD_NBRS: launch_build_nbrs(d, p, bs, s); break;
             case MPS_K_SORT: {

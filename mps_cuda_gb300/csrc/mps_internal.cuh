@@ -371,6 +371,8 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long 
 // three-pass form: A p + dots, x/r update + r.r, direction update (with the loop guard)
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s);
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s);
+// The three-pass update and direction passes in their profiling form (no loop decision).
+void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s);
 void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s);
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);

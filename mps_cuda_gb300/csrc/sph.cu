@@ -814,26 +814,25 @@ __device__ double scene_partial_sum_nt(const Dev& d, const Scene& sc, int c, dou
     return block_sum<NT>(v, sh);
 }
 
-// x += alpha p, r -= alpha Ap, beta = (r.r)_new / (r.r)_old.
+// r -= alpha Ap, beta = (r.r)_new / (r.r)_old.  (x += alpha p is left to k_cg_dir3, which reads p
+// anyway: the same arithmetic, 16 fewer bytes a slot per iteration.)
 template <int NT>
-__global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p) {
+__global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile) {
     constexpr int U = kVecSlots / NT;
     __shared__ double sh[32];
     __shared__ double2 sh2[NT / 32];
     // the grid covers exactly the allocated slots, so the data loads go out before the scene and
     // solver-state lookups (padding slots are loaded and not used)
     const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
-    float4 x[U], r[U], q[U], ap[U];
+    float4 r[U], ap[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int i = i0 + u * NT;
-        x[u] = d.cg_x[i];
         r[u] = d.cg_r[i];
-        q[u] = d.cg_p[i];
         ap[u] = d.cg_ap[i];
     }
     const int s = block_scene(d, kVecSlots);
-    if (!d.solve[s].do_update) return;
+    if (!profile && !d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
     const int end = sc.slot_begin + sc.n;
     const float a = float(d.solve[s].cg_alpha);
@@ -842,9 +841,7 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p) {
     for (int u = 0; u < U; ++u) {
         const int i = i0 + u * NT;
         if (i < end) {
-            x[u].x += a * q[u].x; x[u].y += a * q[u].y; x[u].z += a * q[u].z;
             r[u].x -= a * ap[u].x; r[u].y -= a * ap[u].y; r[u].z -= a * ap[u].z;
-            d.cg_x[i] = x[u];
             d.cg_r[i] = r[u];
             rr += r[u].x * r[u].x + r[u].y * r[u].y + r[u].z * r[u].z;
         }
@@ -856,27 +853,32 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p) {
     if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
 }
 
-// p = r + beta p (MPSCGKernel.cuh:196-207); the loop guard of the WHILE body.
+// x += alpha p with the old direction, then p = r + beta p (MPSCGKernel.cuh:196-207); the loop
+// guard of the WHILE body.
 template <int NT>
 __global__ void __launch_bounds__(NT) k_cg_dir3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
     constexpr int U = kVecSlots / NT;
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
     const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
-    float4 r[U], q[U];
+    float4 x[U], r[U], q[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {   // loads before the lookups, as in k_cg_update3
+        x[u] = d.cg_x[i0 + u * NT];
         r[u] = d.cg_r[i0 + u * NT];
         q[u] = d.cg_p[i0 + u * NT];
     }
     const int s = block_scene(d, kVecSlots);
-    if (!d.solve[s].do_update) return;
+    if (use_cond != 2 && !d.solve[s].do_update) return;   // use_cond 2: profiling form
     const Scene& sc = d.scenes[s];
     const int end = sc.slot_begin + sc.n;
+    const float a = float(d.solve[s].cg_alpha);
     const float b = float(d.solve[s].cg_beta);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int i = i0 + u * NT;
         if (i < end) {
+            x[u].x += a * q[u].x; x[u].y += a * q[u].y; x[u].z += a * q[u].z;
+            d.cg_x[i] = x[u];
             q[u].x = r[u].x + b * q[u].x; q[u].y = r[u].y + b * q[u].y; q[u].z = r[u].z + b * q[u].z;
             d.cg_p[i] = q[u];
         }
@@ -1092,7 +1094,11 @@ void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long con
 }
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     (void)bs;
-    k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p);
+    k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0);
+}
+void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
+    k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 1);
+    k_cg_dir3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0ull, 2, 0);
 }
 void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s) {
