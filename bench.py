@@ -172,10 +172,11 @@ def run_ours(args, scene, rank, world, local_rank):
     ms_max = float(t.item())
     value = scene.n * args.steps * world / (ms_max / 1e3)
     runs = [st1["runs_total"][k] - st0["runs_total"][k] for k in range(3)]
+    passes = [st1["passes_total"][k] - st0["passes_total"][k] for k in range(3)]
     iters = [st1["iters_total"][k] - st0["iters_total"][k] for k in range(3)]
     P = radix_passes(sim)
     static = sim.launches_per_step((0, 0, 0), P)
-    launches = args.steps * static + sim.launches_per_step(tuple(runs), P) - static
+    launches = args.steps * static + sim.launches_per_step(tuple(passes), P) - static
 
     # ---- e2e through the host-buffer C-ABI call (pinned H2D + step + D2H every step), replaying
     # the timed steps from the same starting state
@@ -327,14 +328,17 @@ def run_batched(args, scenes_list, rank, world, local_rank):
     return line
 
 
-def adjoint_launches(sim, K: int, nsteps: int, every: int, passes: int) -> int:
+def adjoint_launches(sim, K: int, nsteps: int, every: int, radix: int, dpasses) -> int:
     """Kernel launches of one forward + reverse: graph steps (forward and segment recompute), the
-    recorded eager step and the reverse kernels of every step."""
-    per_step = sim.launches_per_step((K, K, K), passes)
-    eager = per_step + 2          # recorded step: + solver init/finish around the Jacobi sweeps
-    reverse = 10 + 5 * K          # gather, index, collision, 2K CD, K Jacobi, set-up, ST factor, 2K DF, density x2, scatter, sums
+    recorded eager step and the reverse kernels of every step.  dpasses: the solver passes the
+    steps launched (DF, Jacobi, CD; the stats' passes_total over the run)."""
+    static = sim.launches_per_step((0, 0, 0), radix)
     nseg = (nsteps + every - 1) // every
-    return nsteps * per_step + (nsteps - nseg) * per_step + nsteps * (eager + reverse)
+    nrun = nsteps + (nsteps - nseg) + nsteps       # forward, segment recompute, recorded steps
+    loops = sim.launches_per_step(tuple(dpasses), radix) - static
+    eager_extra = 2               # recorded step: solver init/finish around the Jacobi sweeps
+    reverse = 10 + 5 * K          # gather, index, collision, 2K CD, K Jacobi, set-up, ST factor, 2K DF, density x2, scatter, sums
+    return nrun * static + loops + nsteps * (eager_extra + reverse)
 
 
 def host_gradient_baseline(scene, steps: int = 1):
@@ -468,6 +472,7 @@ def run_adjoint(args, rank, world, local_rank):
     if dist:
         td.barrier()
     e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    sa = sim.stats(check=False)
     with ClockSampler(local_rank) as clk:
         sim.set_fluid(p0, v0)
         e0.record(stream)
@@ -481,6 +486,8 @@ def run_adjoint(args, rank, world, local_rank):
         e3.record(stream)
         e3.synchronize()
     assert L_check == 0
+    sb = sim.stats(check=False)
+    dpasses = [sb["passes_total"][k] - sa["passes_total"][k] for k in range(3)]
     fwd_ms, bwd_ms = e0.elapsed_time(e1), e2.elapsed_time(e3)
     if dist:   # the slowest rank's times; the value counts every rank's particles
         t = torch.tensor([fwd_ms, bwd_ms], dtype=torch.float64, device=dev)
@@ -525,7 +532,7 @@ def run_adjoint(args, rank, world, local_rank):
                 "d2h_bytes_per_step": (32 * n + 32 * n + 32 * n) / horizon,
                 "note": "torch.autograd.Function over the C ABI: initial state in, final state out, cotangents in, "
                         "gradients out, host loss; bytes amortised over the horizon", "same_gradient": same},
-        "gpu_launches": adjoint_launches(sim, K, horizon, every, radix_passes(sim)),
+        "gpu_launches": adjoint_launches(sim, K, horizon, every, radix_passes(sim), dpasses),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -118,7 +118,10 @@ typedef struct mps_stats {
     int64_t boundary_pairs;  /* fluid-boundary neighbour pairs of the step */
     int64_t steps;           /* steps taken since creation */
     int64_t iters_total[3];  /* DF, CG, CD loop counters summed over steps (and scenes) */
-    int64_t runs_total[3];   /* DF, CG, CD loop bodies executed since creation */
+    int64_t runs_total[3];   /* DF, CG, CD solver passes that ran since creation (one per iteration) */
+    int64_t passes_total[3]; /* DF, CG, CD solver passes launched since creation (>= runs_total: a
+                              * graph loop body holds several CG passes; the ones after the stop
+                              * return at once) */
 } mps_stats;
 
 typedef struct mps_handle mps_handle;

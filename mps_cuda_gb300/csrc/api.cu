@@ -447,13 +447,24 @@ int run_phase(mps_handle* h, int phase, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ graph capture
-// Hard bound on the loop bodies of one device-side solve (kind 0 DF, 1 CG, 2 CD): the decision
-// logic ends a loop after at most the iteration cap; this guard ends it two passes later even
-// if that logic failed, and flags the step (bit 2).
+// CG passes per WHILE body.  Each pass's kernels return at once when its scene has stopped, so
+// a body may hold several passes: fewer conditional evaluations (about 3.6 us each on the 1M
+// step) against up to MPSG_CG_UNROLL - 1 empty passes after the stop (1M step: 7.08 ms with 1,
+// 7.02 with 2, 6.99 with 4).
+#ifndef MPSG_CG_UNROLL
+#define MPSG_CG_UNROLL 4
+#endif
+
+// Hard bound on the passes of one device-side solve (kind 0 DF, 1 CG, 2 CD): the decision logic
+// ends a loop after at most the iteration cap, and a CG body runs on to its last pass (the cap
+// rounded up to whole bodies); this guard ends the loop two passes after that even if the
+// decision logic failed, and flags the step (bit 2).
 int loop_limit(const mps_handle* h, int kind) {
     const int cap = h->cfg.fixed_iters > 0 ? h->cfg.fixed_iters : (kind == 1 ? h->cfg.cg_max_iter : h->cfg.max_iter);
-    return cap + 2;
+    const int u = kind == 1 ? MPSG_CG_UNROLL : 1;
+    return (cap + u - 1) / u * u + 2;
 }
+
 
 struct Capture {
     cudaGraph_t g;
@@ -557,15 +568,17 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         {
             Capture b{body, h->cap_stream, {}};
             MPS_CAP_TRY(seg_begin(b));
-            if (p.visc_solver) {
-                launch_jacobi(d, p, bs, hcg, 1, loop_limit(h, 1), nullptr, nullptr, b.s);
-            } else if (p.cg_form == 1) {
-                launch_cg_ap(d, p, bs, hcg, 1, b.s);
-                launch_cg_update(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
-            } else {
-                launch_cg_ap3(d, p, bs, hcg, 1, b.s);
-                launch_cg_update3(d, p, bs, b.s);
-                launch_cg_dir3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+            for (int u = 0; u < MPSG_CG_UNROLL; ++u) {
+                if (p.visc_solver) {
+                    launch_jacobi(d, p, bs, hcg, 1, loop_limit(h, 1), nullptr, nullptr, b.s);
+                } else if (p.cg_form == 1) {
+                    launch_cg_ap(d, p, bs, hcg, 1, b.s);
+                    launch_cg_update(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+                } else {
+                    launch_cg_ap3(d, p, bs, hcg, 1, b.s);
+                    launch_cg_update3(d, p, bs, b.s);
+                    launch_cg_dir3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+                }
             }
             MPS_CAP_TRY(cudaGetLastError());
             MPS_CAP_TRY(seg_end(b));
@@ -991,6 +1004,7 @@ int mps_get_stats(mps_handle* h, mps_stats* out, void* stream) {
     for (int k = 0; k < 3; ++k) {
         out->iters_total[k] = int64_t(c.iters_total[k]);
         out->runs_total[k] = int64_t(c.runs_total[k]);
+        out->passes_total[k] = int64_t(c.passes_total[k]);
     }
     if (c.flags & 1) return fail(MPS_E_OVERFLOW, "neighbour list capacity exceeded");
     if (c.flags & 2) return fail(MPS_E_NONFINITE, "non-finite particle position");

@@ -73,7 +73,8 @@ struct StepCounters {
     int passes;                 // loop bodies run in the current solve (hard guard)
     unsigned long long fluid_pairs, boundary_pairs;
     unsigned long long iters_total[3];  // sum over steps and scenes of the loop counter (DF, CG, CD)
-    unsigned long long runs_total[3];   // loop bodies executed (the graph's WHILE iterations)
+    unsigned long long runs_total[3];   // solver passes that ran (one per iteration; max over scenes)
+    unsigned long long passes_total[3]; // solver passes launched (a graph body holds MPSG_CG_UNROLL CG passes)
 };
 
 // Uniform parameters, passed by value to every kernel.

@@ -386,7 +386,12 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
     const float4 vi = d.vel[i];
     const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
+    if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
+        // a stopped scene's update passes must not run again: a scene that reached its iteration
+        // cap stopped with do_update set for that last update (every block writes the same 0)
+        if (threadIdx.x == 0) d.solve[s].do_update = 0;
+        return;
+    }
     const Scene& sc = d.scenes[s];
     float err = 0.0f;
     if (i < sc.slot_begin + sc.n) {
@@ -524,6 +529,10 @@ __global__ void k_solver_finish(Dev d, Params p, int which) {
     if (threadIdx.x == 0) {
         d.ctr->iters_total[which] += sum;
         d.ctr->runs_total[which] += (unsigned long long)runs;
+        // launched passes: the loop guard's count in graph runs; host-driven loops launch one
+        // pass per iteration and do not count
+        const int launched = d.ctr->passes > 0 ? d.ctr->passes : runs;
+        d.ctr->passes_total[which] += (unsigned long long)launched;
     }
 }
 
@@ -683,7 +692,12 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
     __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
+    if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
+        // a stopped scene's update passes must not run again: a scene that reached its iteration
+        // cap stopped with do_update set for that last update (every block writes the same 0)
+        if (threadIdx.x == 0) d.solve[s].do_update = 0;
+        return;
+    }
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
     float rr = 0.0f, rw = 0.0f;
@@ -760,7 +774,12 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
     const float4 q = d.cg_p[i];
     const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form, no loop decision
+    if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
+        // a stopped scene's update passes must not run again: a scene that reached its iteration
+        // cap stopped with do_update set for that last update (every block writes the same 0)
+        if (threadIdx.x == 0) d.solve[s].do_update = 0;
+        return;
+    }
     const Scene& sc = d.scenes[s];
     float rr = 0.0f, pap = 0.0f;
     if (i < sc.slot_begin + sc.n) {
@@ -897,7 +916,10 @@ __global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long lo
     __shared__ double2 sh2[BS / 32];
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) return;
+    if (use_cond != 2 && !d.solve[s].active) {
+        if (threadIdx.x == 0) d.solve[s].do_update = 0;   // as in k_pressure_A
+        return;
+    }
     const Scene& sc = d.scenes[s];
     const int l = d.solve[s].iter;
     const float4* q = src ? src : (((l - 1) & 1) ? d.cg_p : d.cg_x);

@@ -205,7 +205,8 @@ class Simulation:
         return out
 
     def launches_per_step(self, runs: tuple[int, int, int], radix_passes: int) -> int:
-        """Kernel launches of one graph step given its loop-body counts (DF, CG, CD)."""
+        """Kernel launches of one graph step given its launched solver passes (DF, CG, CD; the
+        stats' passes_total)."""
         # keys + radix (4 per pass) + reorder, lists, [volume], density, DF init + condition
         static = 2 + 4 * radix_passes + 1 + (1 if self.cfg.volume_accumulate else 0) + 1 + 2
         jacobi = self.cfg.visc_solver == L.VISC_JACOBI

@@ -159,6 +159,24 @@ def test_graph_step_equals_eager_phases(mps):
     assert a.stats() ["cd_iters"] == b.stats()["cd_iters"]
 
 
+def test_launched_solver_passes(mps):
+    """Graph steps launch whole CG loop bodies (several passes each; the ones after the stop return
+    at once): passes_total counts them, runs_total the passes that ran.  The DF and CD bodies hold
+    one pass, and the host-driven form launches one pass per iteration."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(10, seed=4)
+    g = Simulation.from_scene(sc)
+    g.step(3)
+    st = g.stats()
+    runs, passes = st["runs_total"], st["passes_total"]
+    assert passes[0] == runs[0] and passes[2] == runs[2]
+    assert runs[1] <= passes[1] < runs[1] + 3 * 4 and passes[1] % 4 == 0
+    e = Simulation.from_scene(sc, use_graph=0)
+    e.step(3)
+    st = e.stats()
+    assert st["passes_total"] == st["runs_total"]
+
+
 def test_deterministic(mps):
     from mps_cuda_gb300 import Simulation, scenes
     sc = scenes.dam_break_small(10, seed=4)
@@ -226,6 +244,23 @@ def test_step_host_matches_device_step(mps):
     b.step_host(p, v, 1)
     pa, va = a.get_fluid()
     assert np.allclose(p, pa, atol=0, rtol=0) or rel_err(p[:, :3], pa[:, :3]) < 1e-6
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_graph_with_cg_cap_equals_host_loop(mps, form):
+    """A CG cap of 5 ends the solve inside a graph loop body (bodies hold several passes): the
+    passes after the cap must change nothing, so the graph steps equal the host-driven loop bit
+    for bit, in both CG forms."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(10, seed=9)
+    g = Simulation.from_scene(sc, cg_max_iter=5, cg_form=form)
+    e = Simulation.from_scene(sc, cg_max_iter=5, cg_form=form, use_graph=0)
+    g.step(2)
+    e.step(2)
+    assert g.stats()["cg_iters"] == e.stats()["cg_iters"]
+    pg, vg = g.get_fluid()
+    pe, ve = e.get_fluid()
+    assert np.array_equal(pg, pe) and np.array_equal(vg, ve)
 
 
 def test_overflow_and_nonfinite_are_reported(mps):
