@@ -194,10 +194,13 @@ enum mps_kernel_id {
     MPS_K_SORT = 5,           /* cell keys + radix sort + reorder */
     MPS_K_CG_VECTOR = 6       /* the three-pass CG's update + direction passes of a CG iteration */
 };
-/* Times `reps` back-to-back launches of one kernel of the step on the current state with CUDA
- * events recorded on `stream`; *ms = mean milliseconds per launch.  Solver passes run in their
- * profiling form (no loop decision) and the B pass moves velocities, so call this after the
- * work being measured.  No counterpart in the reference (it has no device timers). */
+/* Times `reps` (1..1000) launches of one kernel of the step on the current state with CUDA events
+ * recorded on `stream`; *ms = mean milliseconds per launch.  A solver pass is timed with its loop
+ * partner run (untimed) between the timed launches -- pressure A with B, the CG operator with the
+ * CG vector passes, and the reverse -- so that the caches are as inside the solver loop.  Solver
+ * passes run in their profiling form (no loop decision) and change the velocities and CG state,
+ * so call this after the work being measured.  No counterpart in the reference (it has no device
+ * timers). */
 int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream, double* ms);
 
 /* Allocation-free cell sort (no counterpart in the reference).  For callers that cannot

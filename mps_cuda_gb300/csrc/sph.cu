@@ -74,13 +74,14 @@ __device__ __forceinline__ double2 block_sum2_f(float a, float b, double2* sh) {
     return r;
 }
 
-// Deterministic sum of this scene's per-block partials (component c of 2), run by one block.
-template <int BS>
+// Deterministic sum of this scene's per-block partials (component c of 2), run by one block of
+// NT threads over blocks of SPB slots.
+template <int NT, int SPB>
 __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double* sh) {
-    const int b0 = sc.slot_begin / BS, b1 = sc.slot_end / BS;
+    const int b0 = sc.slot_begin / SPB, b1 = sc.slot_end / SPB;
     double v = 0.0;
-    for (int b = b0 + threadIdx.x; b < b1; b += BS) v += __ldcg(d.partial + 2 * b + c);
-    return block_sum<BS>(v, sh);
+    for (int b = b0 + threadIdx.x; b < b1; b += NT) v += __ldcg(d.partial + 2 * b + c);
+    return block_sum<NT>(v, sh);
 }
 
 // Returns true in every thread of the block that is the last of its scene to finish.  Callers
@@ -388,8 +389,9 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
         // a stopped scene's update passes must not run again: a scene that reached its iteration
-        // cap stopped with do_update set for that last update (every block writes the same 0)
-        if (threadIdx.x == 0) d.solve[s].do_update = 0;
+        // cap stopped with do_update set for that last update.  One block per scene clears it
+        // (stores to one address from every block serialise: 27 us for 4000 blocks).
+        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;
         return;
     }
     const Scene& sc = d.scenes[s];
@@ -440,7 +442,7 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
     const double2 bs2 = block_sum2_f<BS>(err, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double tot = scene_partial_sum<BS>(d, sc, 0, sh);
+    const double tot = scene_partial_sum<BS, BS>(d, sc, 0, sh);
     if (threadIdx.x == 0) {
         SceneSolve& S = d.solve[s];
         const double mean = tot / double(sc.n);
@@ -694,8 +696,9 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
         // a stopped scene's update passes must not run again: a scene that reached its iteration
-        // cap stopped with do_update set for that last update (every block writes the same 0)
-        if (threadIdx.x == 0) d.solve[s].do_update = 0;
+        // cap stopped with do_update set for that last update.  One block per scene clears it
+        // (stores to one address from every block serialise: 27 us for 4000 blocks).
+        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;
         return;
     }
     const Scene& sc = d.scenes[s];
@@ -711,8 +714,8 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
     const double2 bs2 = block_sum2_f<BS>(rr, rw, sh2);
     if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
-    const double trw = scene_partial_sum<BS>(d, sc, 1, sh);
+    const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
+    const double trw = scene_partial_sum<BS, BS>(d, sc, 1, sh);
     if (threadIdx.x == 0) {
         SceneSolve& S = d.solve[s];
         const int l = S.iter;
@@ -769,20 +772,22 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
     __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
     const int i = blockIdx.x * BS + threadIdx.x;
-    // own data before the scene and solver-state lookups, as in k_pressure_A
-    const float4 xi = d.pos[i];
-    const float4 q = d.cg_p[i];
-    const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
         // a stopped scene's update passes must not run again: a scene that reached its iteration
-        // cap stopped with do_update set for that last update (every block writes the same 0)
-        if (threadIdx.x == 0) d.solve[s].do_update = 0;
+        // cap stopped with do_update set for that last update.  One block per scene clears it
+        // (stores to one address from every block serialise: 27 us for 4000 blocks).
+        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;
         return;
     }
     const Scene& sc = d.scenes[s];
     float rr = 0.0f, pap = 0.0f;
     if (i < sc.slot_begin + sc.n) {
+        // (the own-slot loads stay after the check: passes after the stop skip them; issuing them
+        // first gained nothing in this kernel)
+        const float4 xi = d.pos[i];
+        const float4 q = d.cg_p[i];
+        const unsigned c = d.cnt[i];
         const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor, xi, q, c);
         d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
         const float4 r = d.cg_r[i];
@@ -792,8 +797,8 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
     const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
     if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
-    const double tpap = scene_partial_sum<BS>(d, sc, 1, sh);
+    const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
+    const double tpap = scene_partial_sum<BS, BS>(d, sc, 1, sh);
     if (threadIdx.x == 0) {
         SceneSolve& S = d.solve[s];
         const int l = S.iter;
@@ -823,15 +828,6 @@ constexpr int kVecSlots = 256;
 #define MPSG_VEC_NT 128
 #endif
 
-// Deterministic sum of this scene's per-block partials (component c of 2) for blocks of SPB slots,
-// run by one block of NT threads.
-template <int NT, int SPB>
-__device__ double scene_partial_sum_nt(const Dev& d, const Scene& sc, int c, double* sh) {
-    const int b0 = sc.slot_begin / SPB, b1 = sc.slot_end / SPB;
-    double v = 0.0;
-    for (int b = b0 + threadIdx.x; b < b1; b += NT) v += __ldcg(d.partial + 2 * b + c);
-    return block_sum<NT>(v, sh);
-}
 
 // r -= alpha Ap, beta = (r.r)_new / (r.r)_old.  (x += alpha p is left to k_cg_dir3, which reads p
 // anyway: the same arithmetic, 16 fewer bytes a slot per iteration.)
@@ -868,7 +864,7 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile)
     const double2 bs2 = block_sum2_f<NT>(rr, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
     if (!last_block_of_scene<kVecSlots>(d, s, sc)) return;
-    const double t = scene_partial_sum_nt<NT, kVecSlots>(d, sc, 0, sh);
+    const double t = scene_partial_sum<NT, kVecSlots>(d, sc, 0, sh);
     if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
 }
 
@@ -917,7 +913,7 @@ __global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long lo
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) {
-        if (threadIdx.x == 0) d.solve[s].do_update = 0;   // as in k_pressure_A
+        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;   // as in k_pressure_A
         return;
     }
     const Scene& sc = d.scenes[s];
@@ -942,7 +938,7 @@ __global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long lo
     const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double trr = scene_partial_sum<BS>(d, sc, 0, sh);
+    const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
     if (threadIdx.x == 0) {
         SceneSolve& S = d.solve[s];
         const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
