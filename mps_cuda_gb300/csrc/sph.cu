@@ -84,6 +84,44 @@ __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double
     return block_sum<NT>(v, sh);
 }
 
+// Deterministic sums of scene sc's per-block partials (both components; blocks of spb slots) by one
+// block of NT threads: kSumILP loads in flight per thread, combined in a fixed order.
+#ifndef MPSG_DECIDE_NT
+#define MPSG_DECIDE_NT 256
+#endif
+#ifndef MPSG_SUM_ILP
+#define MPSG_SUM_ILP 4
+#endif
+constexpr int kDecideThreads = MPSG_DECIDE_NT;
+constexpr int kSumILP = MPSG_SUM_ILP;
+template <int NT>
+__device__ double2 scene_partials(const Dev& d, const Scene& sc, int spb, double* sh) {
+    const int b0 = sc.slot_begin / spb, b1 = sc.slot_end / spb;
+    const double2* P = reinterpret_cast<const double2*>(d.partial);
+    double2 acc[kSumILP];
+#pragma unroll
+    for (int u = 0; u < kSumILP; ++u) acc[u] = make_double2(0.0, 0.0);
+    int b = b0 + int(threadIdx.x);
+    for (; b + (kSumILP - 1) * NT < b1; b += kSumILP * NT) {
+        double2 v[kSumILP];
+#pragma unroll
+        for (int u = 0; u < kSumILP; ++u) v[u] = __ldcg(P + b + u * NT);
+#pragma unroll
+        for (int u = 0; u < kSumILP; ++u) { acc[u].x += v[u].x; acc[u].y += v[u].y; }
+    }
+    for (; b < b1; b += NT) {
+        const double2 v = __ldcg(P + b);
+        acc[0].x += v.x;
+        acc[0].y += v.y;
+    }
+    double2 t = acc[0];
+#pragma unroll
+    for (int u = 1; u < kSumILP; ++u) { t.x += acc[u].x; t.y += acc[u].y; }
+    const double x = block_sum<NT>(t.x, sh);
+    const double y = block_sum<NT>(t.y, sh);
+    return make_double2(x, y);
+}
+
 // Returns true in every thread of the block that is the last of its scene to finish.  Callers
 // write the block's partials from thread 0 just before; the last block reads only those partials,
 // so only thread 0 fences (its partial write before its ticket).  A fence in every thread would
@@ -378,7 +416,6 @@ __global__ void k_set_cond(Dev d, unsigned long long cond) {
 // mode 1: constant density, kappa = rho/rho0 + dt delta - 1 (MPSSPHDFSPHUtil.cuh:259-340).
 template <int BS>
 __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, unsigned long long cond, int use_cond) {
-    __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
     const int i = blockIdx.x * BS + threadIdx.x;
     // the slot's own data loads before the scene and solver-state lookups (the grid covers exactly
@@ -387,13 +424,7 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
     const float4 vi = d.vel[i];
     const unsigned c = d.cnt[i];
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
-        // a stopped scene's update passes must not run again: a scene that reached its iteration
-        // cap stopped with do_update set for that last update.  One block per scene clears it
-        // (stores to one address from every block serialise: 27 us for 4000 blocks).
-        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;
-        return;
-    }
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
     const Scene& sc = d.scenes[s];
     float err = 0.0f;
     if (i < sc.slot_begin + sc.n) {
@@ -441,10 +472,28 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
     }
     const double2 bs2 = block_sum2_f<BS>(err, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
-    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double tot = scene_partial_sum<BS, BS>(d, sc, 0, sh);
+}
+
+// Loop decision of a DF/CD pass (MPSSPHDFSPHUtil.cu:404-433), one block per scene after
+// k_pressure_A: the scene's per-block partials (blocks of bs slots) summed in a fixed order, the
+// mean error, the break rule, the iteration counter; the last scene to decide sets the loop
+// condition.  Deciding in the pass's own last block cost every block a fence and a ticket and
+// left the GPU idle during the last block's sum (about 17 us of a 1M CG operator pass); here the
+// pass kernel's blocks only write their partials.  A stopped scene's do_update is cleared here: a
+// scene that reached its cap stopped with its last update still to run, and the passes after it
+// in the same loop body must not repeat that update.
+__global__ void __launch_bounds__(kDecideThreads) k_pressure_decide(Dev d, Params p, int mode, int bs,
+                                                                    unsigned long long cond, int use_cond) {
+    __shared__ double sh[32];
+    const int s = blockIdx.x;
+    SceneSolve& S = d.solve[s];
+    if (!S.active) {
+        if (threadIdx.x == 0) S.do_update = 0;
+        return;
+    }
+    const Scene& sc = d.scenes[s];
+    const double tot = scene_partials<kDecideThreads>(d, sc, bs, sh).x;
     if (threadIdx.x == 0) {
-        SceneSolve& S = d.solve[s];
         const double mean = tot / double(sc.n);
         const int l = S.iter;
         const double tol = mode == 0 ? p.df_tol_d : p.cd_tol_d;
@@ -769,17 +818,10 @@ __global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p, unsigned long
 // A p, dots r.r and p.Ap, the stop test and alpha = r.r / p.Ap.
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long long cond, int use_cond) {
-    __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
     const int i = blockIdx.x * BS + threadIdx.x;
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
-        // a stopped scene's update passes must not run again: a scene that reached its iteration
-        // cap stopped with do_update set for that last update.  One block per scene clears it
-        // (stores to one address from every block serialise: 27 us for 4000 blocks).
-        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;
-        return;
-    }
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
     const Scene& sc = d.scenes[s];
     float rr = 0.0f, pap = 0.0f;
     if (i < sc.slot_begin + sc.n) {
@@ -796,11 +838,24 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
     }
     const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
     if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
-    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
-    const double tpap = scene_partial_sum<BS, BS>(d, sc, 1, sh);
+}
+
+// The three-pass CG's decision after k_cg_ap3 (one block per scene, as k_pressure_decide): r.r
+// and p.Ap from the partials, the stop test r.r < tol, alpha = r.r / p.Ap, the loop counter
+// (MPSSolver.cuh:33-60).
+__global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, int bs, unsigned long long cond,
+                                                               int use_cond) {
+    __shared__ double sh[32];
+    const int s = blockIdx.x;
+    SceneSolve& S = d.solve[s];
+    if (!S.active) {
+        if (threadIdx.x == 0) S.do_update = 0;
+        return;
+    }
+    const Scene& sc = d.scenes[s];
+    const double2 t = scene_partials<kDecideThreads>(d, sc, bs, sh);
+    const double trr = t.x, tpap = t.y;
     if (threadIdx.x == 0) {
-        SceneSolve& S = d.solve[s];
         const int l = S.iter;
         const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
         const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
@@ -834,7 +889,6 @@ constexpr int kVecSlots = 256;
 template <int NT>
 __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile) {
     constexpr int U = kVecSlots / NT;
-    __shared__ double sh[32];
     __shared__ double2 sh2[NT / 32];
     // the grid covers exactly the allocated slots, so the data loads go out before the scene and
     // solver-state lookups (padding slots are loaded and not used)
@@ -863,9 +917,17 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile)
     }
     const double2 bs2 = block_sum2_f<NT>(rr, 0.0f, sh2);
     if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
-    if (!last_block_of_scene<kVecSlots>(d, s, sc)) return;
-    const double t = scene_partial_sum<NT, kVecSlots>(d, sc, 0, sh);
-    if (threadIdx.x == 0) d.solve[s].cg_beta = t / d.solve[s].rr;
+}
+
+// beta = (r.r)_new / (r.r)_old from k_cg_update3's partials (blocks of kVecSlots slots), one block
+// per scene that is updating.
+__global__ void __launch_bounds__(kDecideThreads) k_cg_beta3(Dev d) {
+    __shared__ double sh[32];
+    const int s = blockIdx.x;
+    SceneSolve& S = d.solve[s];
+    if (!S.do_update) return;
+    const double t = scene_partials<kDecideThreads>(d, d.scenes[s], kVecSlots, sh).x;
+    if (threadIdx.x == 0) S.cg_beta = t / S.rr;
 }
 
 // x += alpha p with the old direction, then p = r + beta p (MPSCGKernel.cuh:196-207); the loop
@@ -1079,6 +1141,7 @@ void launch_set_cond(const Dev& d, unsigned long long cond, cudaStream_t s) {
 void launch_pressure_A(const Dev& d, const Params& p, int mode, int bs, unsigned long long cond, int use_cond,
                        cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_pressure_A, d, p, mode, cond, use_cond);
+    if (use_cond != 2) k_pressure_decide<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, mode, bs, cond, use_cond);
 }
 void launch_pressure_B(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                        cudaStream_t s) {
@@ -1109,10 +1172,12 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long 
 }
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap3, d, p, cond, use_cond);
+    if (use_cond != 2) k_cg_decide3<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, bs, cond, use_cond);
 }
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     (void)bs;
     k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0);
+    k_cg_beta3<<<p.nscenes, kDecideThreads, 0, s>>>(d);
 }
 void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
     k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 1);

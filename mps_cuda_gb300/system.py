@@ -213,8 +213,10 @@ class Simulation:
         # DF finish + solve set-up (ST factor, coefficients + r0, init, condition), solve finish +
         # CD set-up, CD finish + advect
         static += 5 + 4 + 2
-        cg = 1 if jacobi else (2 if self.cfg.cg_form == L.CG_TWO_PASS else 3)
-        return static + 2 * runs[0] + cg * runs[1] + 2 * runs[2]
+        # per pass: pressure A + its decision + pressure B; three-pass CG: operator + decision +
+        # update + beta + direction; two-pass: operator + update; Jacobi: one sweep
+        cg = 1 if jacobi else (2 if self.cfg.cg_form == L.CG_TWO_PASS else 5)
+        return static + 3 * runs[0] + cg * runs[1] + 3 * runs[2]
 
 
 class BatchedSimulation(Simulation):
