@@ -28,6 +28,14 @@ struct XV { float4 x, v; };
 struct XVA { float4 x, v; float2 a; };
 struct XQ { float4 x, q; };
 
+// Programmatic dependent launch between a decide kernel and the vector pass after it: the decide
+// kernel releases its dependent as it starts; the vector pass loads its vectors (written by kernels
+// that completed before the decide kernel started) and waits for the decide kernel's result
+// (griddepcontrol.wait: the primary grid complete and its memory visible) only before it reads
+// alpha or beta and before its first store.  Both instructions are no-ops in a plain launch.
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ int block_scene(const Dev& d, int bs) {
     return d.chunk_scene[(blockIdx.x * bs) / kChunk];
 }
@@ -846,6 +854,7 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
 __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, int bs, unsigned long long cond,
                                                                int use_cond) {
     __shared__ double sh[32];
+    pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
     if (!S.active) {
@@ -879,6 +888,9 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, 
 // flight per thread than one slot a thread.  Blocks keep the 256-slot scene chunks, so the
 // per-block partials and the last-block sum are laid out as for the neighbour kernels.
 constexpr int kVecSlots = 256;
+#ifndef MPSG_VEC_PDL
+#define MPSG_VEC_PDL 1
+#endif
 #ifndef MPSG_VEC_NT
 #define MPSG_VEC_NT 128
 #endif
@@ -900,6 +912,7 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile)
         r[u] = d.cg_r[i];
         ap[u] = d.cg_ap[i];
     }
+    pdl_wait();   // alpha and do_update come from k_cg_decide3
     const int s = block_scene(d, kVecSlots);
     if (!profile && !d.solve[s].do_update) return;
     const Scene& sc = d.scenes[s];
@@ -923,6 +936,7 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile)
 // per scene that is updating.
 __global__ void __launch_bounds__(kDecideThreads) k_cg_beta3(Dev d) {
     __shared__ double sh[32];
+    pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
     if (!S.do_update) return;
@@ -944,6 +958,7 @@ __global__ void __launch_bounds__(NT) k_cg_dir3(Dev d, Params p, unsigned long l
         r[u] = d.cg_r[i0 + u * NT];
         q[u] = d.cg_p[i0 + u * NT];
     }
+    pdl_wait();   // beta comes from k_cg_beta3
     const int s = block_scene(d, kVecSlots);
     if (use_cond != 2 && !d.solve[s].do_update) return;   // use_cond 2: profiling form
     const Scene& sc = d.scenes[s];
@@ -1110,6 +1125,21 @@ int nblocks_for(int n, int bs) { return (n + bs - 1) / bs; }
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
+// Launch with the programmatic-serialisation attribute (see pdl_wait).
+template <class... KArgs, class... Args>
+void launch_after_decide(void (*k)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(unsigned(grid));
+    cfg.blockDim = dim3(unsigned(block));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
 #define MPSG_BS_SWITCH(bs, KERNEL, ...)                                                      \
     do {                                                                                     \
         if ((bs) == 128) KERNEL<128><<<p.slots / 128, 128, 0, s>>>(__VA_ARGS__);             \
@@ -1176,7 +1206,11 @@ void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long con
 }
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     (void)bs;
+#if MPSG_VEC_PDL
+    launch_after_decide(k_cg_update3<MPSG_VEC_NT>, p.slots / kVecSlots, MPSG_VEC_NT, s, d, p, 0);
+#else
     k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0);
+#endif
     k_cg_beta3<<<p.nscenes, kDecideThreads, 0, s>>>(d);
 }
 void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
@@ -1186,7 +1220,11 @@ void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
 void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s) {
     (void)bs;
+#if MPSG_VEC_PDL
+    launch_after_decide(k_cg_dir3<MPSG_VEC_NT>, p.slots / kVecSlots, MPSG_VEC_NT, s, d, p, cond, use_cond, limit);
+#else
     k_cg_dir3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, cond, use_cond, limit);
+#endif
 }
 void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                    const float4* src, float4* dst, cudaStream_t s) {
