@@ -69,6 +69,7 @@ struct SceneSolve {
 struct StepCounters {
     unsigned int scenes_done;   // scenes whose last block finished this pass
     int nactive;                // scenes active at the start of the pass
+    int nactive_next;           // scenes still active after their decision in the current pass
     int flags;                  // bit0 overflow, bit1 non-finite
     int passes;                 // loop bodies run in the current solve (hard guard)
     unsigned long long fluid_pairs, boundary_pairs;

@@ -148,16 +148,19 @@ __device__ bool last_block_of_scene(const Dev& d, int s, const Scene& sc) {
     return am_last != 0;
 }
 
-// Called by thread 0 of the last block of each active scene after its decision: the last
-// scene to decide counts the scenes still active and sets the loop condition.
-__device__ void finish_scene_decision(const Dev& d, const Params& p, unsigned long long cond, int use_cond) {
+// Called by thread 0 of the block that decided a scene, after the decision: a scene still active
+// counts itself, and the last scene to decide takes the count (resetting it for the next pass)
+// and sets the loop condition.  (Counting the active flags of every scene there instead was a
+// serial chain of one load per scene, 256 a pass for the batched workload.)
+__device__ void finish_scene_decision(const Dev& d, const Params& p, unsigned long long cond, int use_cond,
+                                      int still_active) {
+    if (still_active) atomicAdd(&d.ctr->nactive_next, 1);
     __threadfence();
     const unsigned t = atomicAdd(&d.ctr->scenes_done, 1u);
     const int nact = *reinterpret_cast<volatile int*>(&d.ctr->nactive);
     if (t == unsigned(nact) - 1u) {
         __threadfence();
-        int cnt = 0;
-        for (int s = 0; s < p.nscenes; ++s) cnt += *reinterpret_cast<volatile int*>(&d.solve[s].active);
+        const int cnt = atomicExch(&d.ctr->nactive_next, 0);
         d.ctr->nactive = cnt;
         d.ctr->scenes_done = 0;
         if (use_cond) cudaGraphSetConditional(cond, cnt > 0 ? 1u : 0u);
@@ -410,6 +413,7 @@ __global__ void k_solver_init(Dev d, Params p) {
     __syncthreads();
     if (threadIdx.x == 0) {
         d.ctr->nactive = cnt;
+        d.ctr->nactive_next = 0;
         d.ctr->scenes_done = 0;
         d.ctr->passes = 0;
     }
@@ -517,7 +521,7 @@ __global__ void __launch_bounds__(kDecideThreads) k_pressure_decide(Dev d, Param
             S.iter = l + 1;
             if (l + 1 > cap) S.active = 0;
         }
-        finish_scene_decision(d, p, cond, use_cond);
+        finish_scene_decision(d, p, cond, use_cond, S.active);
     }
 }
 
@@ -792,7 +796,7 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
             if (l + 1 > cap) S.active = 0;
         }
         S.rr = trr;
-        finish_scene_decision(d, p, cond, use_cond);
+        finish_scene_decision(d, p, cond, use_cond, S.active);
     }
 }
 
@@ -879,7 +883,7 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, 
             S.iter = l + 1;
             if (l + 1 > cap) S.active = 0;
         }
-        finish_scene_decision(d, p, cond, use_cond);
+        finish_scene_decision(d, p, cond, use_cond, S.active);
     }
 }
 
@@ -1030,7 +1034,7 @@ __global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long lo
             S.iter = l + 1;
             if (l + 1 > cap) S.active = 0;
         }
-        finish_scene_decision(d, p, cond, use_cond);
+        finish_scene_decision(d, p, cond, use_cond, S.active);
     }
 }
 
