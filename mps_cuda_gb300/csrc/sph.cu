@@ -82,13 +82,41 @@ __device__ __forceinline__ double2 block_sum2_f(float a, float b, double2* sh) {
     return r;
 }
 
+// Per-block partials are stored as FP32 (hi, lo) pairs, hi + lo = the block's FP64 sum to 48 bits
+// (16 bytes a block: two components), and the one-block scene sums add them as compensated
+// FP32 pairs (TwoSum, then renormalised): with GB300's FP64 rate, adding a 1M scene's 7800
+// partials in FP64 on one SM was most of a decide kernel.  Sums are deterministic (fixed order)
+// and relative errors stay near 1e-12, far below the FP32 rounding of alpha and beta.
+__device__ __forceinline__ float2 df_from(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - double(h)));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = __fadd_rn(a.x, b.x);
+    const float v = __fsub_rn(s, a.x);
+    const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, v)), __fsub_rn(b.x, v));
+    const float t = __fadd_rn(e, __fadd_rn(a.y, b.y));
+    const float h = __fadd_rn(s, t);
+    return make_float2(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ double df_to(float2 a) { return double(a.x) + double(a.y); }
+// Thread 0 of block b stores its partials (components 0 and 1).
+__device__ __forceinline__ void put_partial(const Dev& d, int b, double v0, double v1) {
+    const float2 a = df_from(v0), c = df_from(v1);
+    reinterpret_cast<float4*>(d.partial)[b] = make_float4(a.x, a.y, c.x, c.y);
+}
+
 // Deterministic sum of this scene's per-block partials (component c of 2), run by one block of
 // NT threads over blocks of SPB slots.
 template <int NT, int SPB>
 __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double* sh) {
     const int b0 = sc.slot_begin / SPB, b1 = sc.slot_end / SPB;
     double v = 0.0;
-    for (int b = b0 + threadIdx.x; b < b1; b += NT) v += __ldcg(d.partial + 2 * b + c);
+    const float4* P = reinterpret_cast<const float4*>(d.partial);
+    for (int b = b0 + threadIdx.x; b < b1; b += NT) {
+        const float4 q = __ldcg(P + b);
+        v += c == 0 ? df_to(make_float2(q.x, q.y)) : df_to(make_float2(q.z, q.w));
+    }
     return block_sum<NT>(v, sh);
 }
 
@@ -102,32 +130,58 @@ __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double
 #endif
 constexpr int kDecideThreads = MPSG_DECIDE_NT;
 constexpr int kSumILP = MPSG_SUM_ILP;
-template <int NT>
-__device__ double2 scene_partials(const Dev& d, const Scene& sc, int spb, double* sh) {
+// Deterministic sums of scene sc's per-block partials (blocks of spb slots; component 0, or both
+// when NC = 2) by one block of NT threads: kSumILP loads in flight per thread, combined in a fixed
+// order.
+template <int NT, int NC>
+__device__ double2 scene_partials(const Dev& d, const Scene& sc, int spb, double2* sh) {
     const int b0 = sc.slot_begin / spb, b1 = sc.slot_end / spb;
-    const double2* P = reinterpret_cast<const double2*>(d.partial);
-    double2 acc[kSumILP];
+    const float4* P = reinterpret_cast<const float4*>(d.partial);
+    float2 ax[kSumILP], ay[kSumILP];
 #pragma unroll
-    for (int u = 0; u < kSumILP; ++u) acc[u] = make_double2(0.0, 0.0);
+    for (int u = 0; u < kSumILP; ++u) { ax[u] = make_float2(0.f, 0.f); ay[u] = make_float2(0.f, 0.f); }
     int b = b0 + int(threadIdx.x);
     for (; b + (kSumILP - 1) * NT < b1; b += kSumILP * NT) {
-        double2 v[kSumILP];
+        float4 v[kSumILP];
 #pragma unroll
         for (int u = 0; u < kSumILP; ++u) v[u] = __ldcg(P + b + u * NT);
 #pragma unroll
-        for (int u = 0; u < kSumILP; ++u) { acc[u].x += v[u].x; acc[u].y += v[u].y; }
+        for (int u = 0; u < kSumILP; ++u) {
+            ax[u] = df_add(ax[u], make_float2(v[u].x, v[u].y));
+            if (NC == 2) ay[u] = df_add(ay[u], make_float2(v[u].z, v[u].w));
+        }
     }
     for (; b < b1; b += NT) {
-        const double2 v = __ldcg(P + b);
-        acc[0].x += v.x;
-        acc[0].y += v.y;
+        const float4 v = __ldcg(P + b);
+        ax[0] = df_add(ax[0], make_float2(v.x, v.y));
+        if (NC == 2) ay[0] = df_add(ay[0], make_float2(v.z, v.w));
     }
-    double2 t = acc[0];
+    float2 tx = ax[0], ty = ay[0];
 #pragma unroll
-    for (int u = 1; u < kSumILP; ++u) { t.x += acc[u].x; t.y += acc[u].y; }
-    const double x = block_sum<NT>(t.x, sh);
-    const double y = block_sum<NT>(t.y, sh);
-    return make_double2(x, y);
+    for (int u = 1; u < kSumILP; ++u) {
+        tx = df_add(tx, ax[u]);
+        if (NC == 2) ty = df_add(ty, ay[u]);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tx = df_add(tx, make_float2(__shfl_down_sync(kFull, tx.x, o), __shfl_down_sync(kFull, tx.y, o)));
+        if (NC == 2) ty = df_add(ty, make_float2(__shfl_down_sync(kFull, ty.x, o), __shfl_down_sync(kFull, ty.y, o)));
+    }
+    float4* sw = reinterpret_cast<float4*>(sh);
+    if (lane == 0) sw[warp] = make_float4(tx.x, tx.y, ty.x, ty.y);
+    __syncthreads();
+    if (warp == 0) {
+        const float4 w = lane < NT / 32 ? sw[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        tx = make_float2(w.x, w.y);
+        ty = make_float2(w.z, w.w);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tx = df_add(tx, make_float2(__shfl_down_sync(kFull, tx.x, o), __shfl_down_sync(kFull, tx.y, o)));
+            if (NC == 2) ty = df_add(ty, make_float2(__shfl_down_sync(kFull, ty.x, o), __shfl_down_sync(kFull, ty.y, o)));
+        }
+    }
+    return make_double2(df_to(tx), NC == 2 ? df_to(ty) : 0.0);   // valid in thread 0
 }
 
 // Returns true in every thread of the block that is the last of its scene to finish.  Callers
@@ -154,6 +208,11 @@ __device__ bool last_block_of_scene(const Dev& d, int s, const Scene& sc) {
 // serial chain of one load per scene, 256 a pass for the batched workload.)
 __device__ void finish_scene_decision(const Dev& d, const Params& p, unsigned long long cond, int use_cond,
                                       int still_active) {
+    if (p.nscenes == 1) {   // the only scene is the last to decide; kernel boundaries order the rest
+        d.ctr->nactive = still_active;
+        if (use_cond) cudaGraphSetConditional(cond, still_active ? 1u : 0u);
+        return;
+    }
     if (still_active) atomicAdd(&d.ctr->nactive_next, 1);
     __threadfence();
     const unsigned t = atomicAdd(&d.ctr->scenes_done, 1u);
@@ -483,7 +542,7 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         if (d.tape_code) d.tape_code[i] = code;
     }
     const double2 bs2 = block_sum2_f<BS>(err, 0.0f, sh2);
-    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
+    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, 0.0);
 }
 
 // Loop decision of a DF/CD pass (MPSSPHDFSPHUtil.cu:404-433), one block per scene after
@@ -496,7 +555,7 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
 // in the same loop body must not repeat that update.
 __global__ void __launch_bounds__(kDecideThreads) k_pressure_decide(Dev d, Params p, int mode, int bs,
                                                                     unsigned long long cond, int use_cond) {
-    __shared__ double sh[32];
+    __shared__ double2 sh[32];
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
     if (!S.active) {
@@ -504,7 +563,7 @@ __global__ void __launch_bounds__(kDecideThreads) k_pressure_decide(Dev d, Param
         return;
     }
     const Scene& sc = d.scenes[s];
-    const double tot = scene_partials<kDecideThreads>(d, sc, bs, sh).x;
+    const double tot = scene_partials<kDecideThreads, 1>(d, sc, bs, sh).x;
     if (threadIdx.x == 0) {
         const double mean = tot / double(sc.n);
         const int l = S.iter;
@@ -773,7 +832,7 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
         rw = r.x * w.x + r.y * w.y + r.z * w.z;
     }
     const double2 bs2 = block_sum2_f<BS>(rr, rw, sh2);
-    if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
+    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, bs2.y);
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
     const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
     const double trw = scene_partial_sum<BS, BS>(d, sc, 1, sh);
@@ -849,7 +908,7 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
         pap = q.x * a.x + q.y * a.y + q.z * a.z;
     }
     const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
-    if (threadIdx.x == 0) { d.partial[2 * blockIdx.x] = bs2.x; d.partial[2 * blockIdx.x + 1] = bs2.y; }
+    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, bs2.y);
 }
 
 // The three-pass CG's decision after k_cg_ap3 (one block per scene, as k_pressure_decide): r.r
@@ -857,7 +916,7 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
 // (MPSSolver.cuh:33-60).
 __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, int bs, unsigned long long cond,
                                                                int use_cond) {
-    __shared__ double sh[32];
+    __shared__ double2 sh[32];
     pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
@@ -866,7 +925,7 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, 
         return;
     }
     const Scene& sc = d.scenes[s];
-    const double2 t = scene_partials<kDecideThreads>(d, sc, bs, sh);
+    const double2 t = scene_partials<kDecideThreads, 2>(d, sc, bs, sh);
     const double trr = t.x, tpap = t.y;
     if (threadIdx.x == 0) {
         const int l = S.iter;
@@ -933,18 +992,18 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile)
         }
     }
     const double2 bs2 = block_sum2_f<NT>(rr, 0.0f, sh2);
-    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
+    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, 0.0);
 }
 
 // beta = (r.r)_new / (r.r)_old from k_cg_update3's partials (blocks of kVecSlots slots), one block
 // per scene that is updating.
 __global__ void __launch_bounds__(kDecideThreads) k_cg_beta3(Dev d) {
-    __shared__ double sh[32];
+    __shared__ double2 sh[32];
     pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
     if (!S.do_update) return;
-    const double t = scene_partials<kDecideThreads>(d, d.scenes[s], kVecSlots, sh).x;
+    const double t = scene_partials<kDecideThreads, 1>(d, d.scenes[s], kVecSlots, sh).x;
     if (threadIdx.x == 0) S.cg_beta = t / S.rr;
 }
 
@@ -1017,7 +1076,7 @@ __global__ void __launch_bounds__(BS) k_jacobi(Dev d, Params p, unsigned long lo
                             qi.z + (m2.x * rx + m2.y * ry + m.z * rz), 0.0f);
     }
     const double2 bs2 = block_sum2_f<BS>(rr, 0.0f, sh2);
-    if (threadIdx.x == 0) d.partial[2 * blockIdx.x] = bs2.x;
+    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, 0.0);
     if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
     const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
     if (threadIdx.x == 0) {
