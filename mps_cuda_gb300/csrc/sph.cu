@@ -123,7 +123,7 @@ __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double
 // Deterministic sums of scene sc's per-block partials (both components; blocks of spb slots) by one
 // block of NT threads: kSumILP loads in flight per thread, combined in a fixed order.
 #ifndef MPSG_DECIDE_NT
-#define MPSG_DECIDE_NT 256
+#define MPSG_DECIDE_NT 1024
 #endif
 #ifndef MPSG_SUM_ILP
 #define MPSG_SUM_ILP 4
