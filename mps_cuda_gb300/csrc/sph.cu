@@ -811,16 +811,9 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
 // r.r < tol and loop counter (MPSSolver.cuh:33-60); r0 = b - A x0 comes from k_cg_b.
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long long cond, int use_cond) {
-    __shared__ double sh[32];
     __shared__ double2 sh2[BS / 32];
     const int s = block_scene(d, BS);
-    if (use_cond != 2 && !d.solve[s].active) {   // use_cond 2: profiling form, no loop decision
-        // a stopped scene's update passes must not run again: a scene that reached its iteration
-        // cap stopped with do_update set for that last update.  One block per scene clears it
-        // (stores to one address from every block serialise: 27 us for 4000 blocks).
-        if (threadIdx.x == 0 && int(blockIdx.x) * BS == d.scenes[s].slot_begin) d.solve[s].do_update = 0;
-        return;
-    }
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
     const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
     float rr = 0.0f, rw = 0.0f;
@@ -833,11 +826,24 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
     }
     const double2 bs2 = block_sum2_f<BS>(rr, rw, sh2);
     if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, bs2.y);
-    if (use_cond == 2 || !last_block_of_scene<BS>(d, s, sc)) return;
-    const double trr = scene_partial_sum<BS, BS>(d, sc, 0, sh);
-    const double trw = scene_partial_sum<BS, BS>(d, sc, 1, sh);
+}
+
+// The two-pass CG's decision after k_cg_ap (one block per scene, as k_cg_decide3): r.r and r.w,
+// the stop test, beta = (r.r) / (r.r)_old and alpha = (r.r) / (r.w - beta (r.r) / alpha_old)
+// (first iteration: beta = 0, alpha = (r.r) / (r.w)).
+__global__ void __launch_bounds__(kDecideThreads) k_cg_decide2(Dev d, Params p, int bs, unsigned long long cond,
+                                                               int use_cond) {
+    __shared__ double2 sh[32];
+    pdl_release();
+    const int s = blockIdx.x;
+    SceneSolve& S = d.solve[s];
+    if (!S.active) {
+        if (threadIdx.x == 0) S.do_update = 0;
+        return;
+    }
+    const double2 t = scene_partials<kDecideThreads, 2>(d, d.scenes[s], bs, sh);
+    const double trr = t.x, trw = t.y;
     if (threadIdx.x == 0) {
-        SceneSolve& S = d.solve[s];
         const int l = S.iter;
         const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
         const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
@@ -864,18 +870,20 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
     if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
-    const int s = block_scene(d, BS);
-    if (!d.solve[s].do_update) return;
-    const Scene& sc = d.scenes[s];
     const int i = blockIdx.x * BS + threadIdx.x;
-    if (i >= sc.slot_begin + sc.n) return;
-    const float a = float(d.solve[s].cg_alpha);
-    const float b = float(d.solve[s].cg_beta);
+    // the vectors load before the wait for k_cg_decide2 (the grid covers exactly the allocated slots)
     const float4 r = d.cg_r[i];
     const float4 w = d.cg_ap[i];
     float4 q = d.cg_p[i];
     float4 sv = d.cg_s[i];
     float4 x = d.cg_x[i];
+    pdl_wait();
+    const int s = block_scene(d, BS);
+    if (!d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    if (i >= sc.slot_begin + sc.n) return;
+    const float a = float(d.solve[s].cg_alpha);
+    const float b = float(d.solve[s].cg_beta);
     q.x = r.x + b * q.x; q.y = r.y + b * q.y; q.z = r.z + b * q.z;
     sv.x = w.x + b * sv.x; sv.y = w.y + b * sv.y; sv.z = w.z + b * sv.z;
     x.x += a * q.x; x.y += a * q.y; x.z += a * q.z;
@@ -1254,6 +1262,7 @@ void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 }
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
+    if (use_cond != 2) k_cg_decide2<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, bs, cond, use_cond);
 }
 // The CG's vector passes stream their arrays; they run with 256-thread blocks whatever the
 // neighbour passes use (half the per-block partials for the residual sums; scenes are padded to
@@ -1261,7 +1270,7 @@ void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond
 void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                       cudaStream_t s) {
     (void)bs;
-    MPSG_BS_SWITCH(256, k_cg_update, d, p, cond, use_cond, limit);
+    launch_after_decide(k_cg_update<256>, p.slots / 256, 256, s, d, p, cond, use_cond, limit);
 }
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap3, d, p, cond, use_cond);

@@ -214,8 +214,8 @@ class Simulation:
         # CD set-up, CD finish + advect
         static += 5 + 4 + 2
         # per pass: pressure A + its decision + pressure B; three-pass CG: operator + decision +
-        # update + beta + direction; two-pass: operator + update; Jacobi: one sweep
-        cg = 1 if jacobi else (2 if self.cfg.cg_form == L.CG_TWO_PASS else 5)
+        # update + beta + direction; two-pass: operator + decision + update; Jacobi: one sweep
+        cg = 1 if jacobi else (3 if self.cfg.cg_form == L.CG_TWO_PASS else 5)
         return static + 3 * runs[0] + cg * runs[1] + 3 * runs[2]
 
 
