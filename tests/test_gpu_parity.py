@@ -9,6 +9,8 @@ Tolerances (FP32 bulk vs FP64 oracle, same inputs):
 Solver phases are compared in fixed-iteration mode (same number of Jacobi / CG iterations on
 both sides) and, in adaptive mode, by iteration counts within one iteration.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -289,6 +291,49 @@ def test_empty_boundary_and_out_of_box_particles(mps, orc):
     o.step(1)
     p, v = sim.get_fluid()
     assert rel_err(p[:, :3], o.get("pos")) < 1e-6
+
+
+def test_single_particle_and_single_pair(mps, orc):
+    """The smallest inputs: one fluid particle (no fluid neighbours) and two (one pair) against the
+    oracle over two full steps."""
+    base = scenes_mod().dam_break_small(4, seed=3)
+    for keep in ([0], [0, 1]):
+        sc = dataclasses.replace(base, pos4=base.pos4[keep].copy(), vel4=base.vel4[keep].copy(),
+                                 name=f"tiny_{len(keep)}")
+        sim, o = make(mps, orc, sc)
+        sim.step(2)
+        o.step(2)
+        p, v = sim.get_fluid()
+        assert rel_err(p[:, :3], o.get("pos")) < 1e-6, keep
+        assert rel_err(v[:, :3], o.get("vel")) < 1e-4, keep
+
+
+def test_batched_with_an_empty_scene(mps):
+    """A scene without fluid particles in the middle of a batch: the other scenes step exactly as
+    they do alone."""
+    from mps_cuda_gb300 import BatchedSimulation, Simulation
+    scs = scenes_mod().batched_scenes(3, seed=5, nmin=500, nmax=2000)
+    empty = dataclasses.replace(scs[1], pos4=scs[1].pos4[:0].copy(), vel4=scs[1].vel4[:0].copy())
+    batch = [scs[0], empty, scs[2]]
+    b = BatchedSimulation(batch)
+    b.step(2)
+    pb, vb = b.get_fluid()
+    its = b.scene_iters()
+    off = 0
+    for k, sc in enumerate(batch):
+        if sc.n:
+            s = Simulation.from_scene(sc)
+            s.step(2)
+            p, v = s.get_fluid()
+            assert np.array_equal(p, pb[off:off + sc.n]) and np.array_equal(v, vb[off:off + sc.n]), k
+            st = s.stats()
+            assert (st["df_iters"], st["cg_iters"], st["cd_iters"]) == tuple(its[k]), k
+        off += sc.n
+
+
+def scenes_mod():
+    from mps_cuda_gb300 import scenes
+    return scenes
 
 
 @pytest.mark.parametrize("fixed", [0, 6])
