@@ -70,6 +70,7 @@ struct AdjointStore {
     float4 *gx = nullptr, *gv = nullptr, *gx_id = nullptr, *gv_id = nullptr;
     float4 *qbar0 = nullptr, *qbar1 = nullptr, *bbar = nullptr, *gg = nullptr;
     float4 *Dbar = nullptr, *Dbar2 = nullptr;   // symmetric 3x3 cotangent of the Jacobi block: (xx, yy, zz, xy), (xz, yz)
+    float4 *y0 = nullptr, *y1 = nullptr;        // D^-1 qbar of a reverse sweep's input / output
     float *grho = nullptr, *galpha = nullptr, *gdelta = nullptr, *gsf = nullptr;
     double *gsig = nullptr, *gmu = nullptr;   // per-slot parameter cotangents (FP64)
     float2* pc = nullptr;            // per pair (cbar, cvbar), interleaved like nbr_f
@@ -83,7 +84,7 @@ struct AdjointStore {
         void* ptrs[] = {cp_pos, cp_vel, cp_ids, fin_pos, fin_vel, fin_ids, t_udf, t_ucd, t_q, t_x, t_kdf, t_kcd,
                         t_cdf, t_ccd, t_adv, t_nbrf, t_nbrb, t_cnt, t_ids, t_coef, t_aux, t_jd, t_jd2, t_rho,
                         t_alpha, gx, gv, gx_id, gv_id, qbar0, qbar1, bbar,
-                        Dbar, Dbar2, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
+                        Dbar, Dbar2, y0, y1, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         *this = AdjointStore{};
@@ -192,7 +193,7 @@ constexpr int kAdjBatch = 2;
 struct AG { float4 x, g; float k, m; };          // pass A: position, velocity cotangent, stiffness, mass
 struct BG { float4 x, u; };                      // pass B: position, velocity (w: delta cotangent)
 struct JS { float2 c; unsigned rv; };            // Jacobi reverse, streamed: own coefficient, reverse index
-struct JG { float4 x, qb, d, d2, q; float2 cji; };
+struct JG { float4 x, y, q; float2 cji; };
 
 __device__ __forceinline__ bool slot_live(const Dev& d, int i, int& s) {
     s = d.chunk_scene[i / kChunk];
@@ -386,10 +387,22 @@ __global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X
 // ------------------------------------------------------------------ Jacobi solve reverse
 // One transposed sweep: y = qbar / D, qbar' = qbar - (A_0 + f I)^T y, plus the sweep's share of
 // the cotangents of b, D and of each pair's coefficients (c, cv) and explicit x_ij.
+// y = D^-1 qbar for every live slot: the first reverse sweep's input (later sweeps write the
+// next sweep's y themselves, so that a sweep gathers a neighbour's y instead of its qbar and
+// 3x3 block).
+__global__ void __launch_bounds__(kAB) k_adj_y(Dev d, Params p, const float4* qbar, float4* y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const float3 v = sym_mul(d.jac_d[i], d.jac_d2[i], f3(qbar[i]));
+    y[i] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+
 __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float4* X, const unsigned char* rev,
                                                      const float4* qk, const float4* qk1, const float4* qbar,
-                                                     float4* qbar_out, float4* bbar, float4* Dbar, float4* Dbar2,
-                                                     float2* pc, float4* px) {
+                                                     float4* qbar_out, const float4* yin, float4* yout, float4* bbar,
+                                                     float4* Dbar, float4* Dbar2, float2* pc, float4* px) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.slots) return;
     int s;
@@ -397,14 +410,14 @@ __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float
     const size_t S = size_t(p.slots);
     const float4 xi = X[i];
     const float4 qb = qbar[i];
-    const float3 y = sym_mul(d.jac_d[i], d.jac_d2[i], f3(qb));
+    const float3 y = f3(yin[i]);   // D_i^-1 qbar_i (yin: every slot's, written by the previous sweep)
     const float3 qi = f3(qk[i]);
     const int nf = int(d.cnt[i] & 0xffffu);
     float3 aty = (1.0f + p.cg_factor) * y;
     visit2<kAdjBatch, JS, JG>(d.nbr_f, S, i, nf,
         [&](int k) { const size_t at = size_t(k) * S + size_t(i); return JS{d.cg_coef[at], unsigned(rev[at])}; },
         [&](unsigned j, const JS& st, int) {
-            return JG{X[j], qbar[j], d.jac_d[j], d.jac_d2[j], qk[j],
+            return JG{X[j], yin[j], qk[j],
                       st.rv != 255u ? d.cg_coef[size_t(st.rv) * S + j] : make_float2(0.f, 0.f)};
         },
         [&](const JG& t, const JS& st, int k) {
@@ -416,7 +429,7 @@ __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float
         aty += p.dt * (cij.x * y - (cij.y * ye) * e);
         if (st.rv != 255u) {
             const float2 cji = t.cji;
-            const float3 yj = sym_mul(t.d, t.d2, f3(t.qb));
+            const float3 yj = f3(t.y);
             const float yje = dot3(yj, e);
             aty -= p.dt * (cji.x * yj - (cji.y * yje) * e);
         }
@@ -431,7 +444,10 @@ __global__ void __launch_bounds__(kAB) k_adj_jacobi(Dev d, Params p, const float
         b.x += tt.x; b.y += tt.y; b.z += tt.z;
         px[at] = b;
     });
-    qbar_out[i] = make_float4(qb.x - aty.x, qb.y - aty.y, qb.z - aty.z, 0.0f);
+    const float3 qn = make_float3(qb.x - aty.x, qb.y - aty.y, qb.z - aty.z);
+    qbar_out[i] = make_float4(qn.x, qn.y, qn.z, 0.0f);
+    const float3 yn = sym_mul(d.jac_d[i], d.jac_d2[i], qn);   // the next sweep's y_i
+    yout[i] = make_float4(yn.x, yn.y, yn.z, 0.0f);
     float4 bb = bbar[i];
     bb.x += y.x; bb.y += y.y; bb.z += y.z;
     bbar[i] = bb;
@@ -802,7 +818,7 @@ size_t store_bytes(const mps_handle* h, int nsteps, int every) {
     step += (cap + capb + 2) * S * sizeof(unsigned) + cap * S * sizeof(float2);   // lists, counts, ids, coefficients
     step += S * (sizeof(float2) + 2 * sizeof(float4) + 2 * sizeof(float));      // aux, Jacobi blocks, rho, alpha
     b += E * step;
-    b += 10 * S * sizeof(float4) + 4 * S * sizeof(float) + 2 * S * sizeof(double);   // cotangents
+    b += 12 * S * sizeof(float4) + 4 * S * sizeof(float) + 2 * S * sizeof(double);   // cotangents
     b += cap * S * (sizeof(float2) + sizeof(float4) + 1);   // per-pair cotangents + reverse index
     b += size_t(h->nscenes) * 2 * sizeof(double) + 64;
     return b;
@@ -858,7 +874,7 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     ADJ_TRY(alloc(&A.t_jd2, E * S, t));
     ADJ_TRY(alloc(&A.t_rho, E * S, t));
     ADJ_TRY(alloc(&A.t_alpha, E * S, t));
-    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.Dbar2, &A.gg};
+    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.Dbar2, &A.gg, &A.y0, &A.y1};
     for (float4** q : f4) ADJ_TRY(alloc(q, S, t));
     ADJ_TRY(alloc(&A.gx_id, size_t(std::max<int64_t>(h->n, 1)), t));
     ADJ_TRY(alloc(&A.gv_id, size_t(std::max<int64_t>(h->n, 1)), t));
@@ -1043,10 +1059,14 @@ int adjoint_step(mps_handle* h, const Slot& t, cudaStream_t s) {
     ADJ_TRY(cudaMemcpyAsync(A.qbar0, A.gv, S * sizeof(float4), cudaMemcpyDeviceToDevice, s));
     float4* qa = A.qbar0;
     float4* qb = A.qbar1;
+    float4* ya = A.y0;
+    float4* yb = A.y1;
+    k_adj_y<<<nb, kAB, 0, s>>>(d, p, qa, ya);
     for (int k = K - 1; k >= 0; --k) {
         k_adj_jacobi<<<nb, kAB, 0, s>>>(d, p, t.x, A.rev, t.q + size_t(k) * S, t.q + size_t(k + 1) * S, qa, qb,
-                                         A.bbar, A.Dbar, A.Dbar2, A.pc, A.px);
+                                         ya, yb, A.bbar, A.Dbar, A.Dbar2, A.pc, A.px);
         std::swap(qa, qb);
+        std::swap(ya, yb);
     }
     const float4* V0 = t.udf + size_t(K) * S;   // pre-solve velocity = DF output
     k_adj_visc_coef<<<nb, kAB, 0, s>>>(d, p, t.x, V0, A.rev, qa, A.bbar, A.Dbar, A.Dbar2, A.pc, A.px, A.gv, A.gx,
