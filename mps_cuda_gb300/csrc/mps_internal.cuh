@@ -40,6 +40,9 @@ struct Scene {
 // thread block gathers from from about 10x to about 6x its own cells.  grid_key is the key inside
 // one grid (ny and nz padded to whole columns); cell_key adds the scene's key base.
 constexpr unsigned kBrick = 2;
+#ifndef MPSG_KEY_ORDER
+#define MPSG_KEY_ORDER 1   // 1: neighbour lists in ascending cell-key (slot) order; 0: (dz, dy, dx) order
+#endif
 __host__ __device__ __forceinline__ unsigned long long grid_key(int nx, int ny, int cx, int cy, int cz) {
     const unsigned nyb = (unsigned(ny) + kBrick - 1) / kBrick;
     const unsigned long long col = (unsigned long long)(unsigned(cz) / kBrick) * nyb + unsigned(cy) / kBrick;

@@ -294,6 +294,17 @@ __device__ __forceinline__ bool fluid_cell(const Dev& d, int slots, unsigned lon
 }
 
 // ------------------------------------------------------------------ neighbour lists
+// The 27 neighbour cells of a cell in ascending key order, for the four positions of the cell in
+// its 2 x 2 column (case = (cy & 1) | (cz & 1) << 1); entry = (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4.
+// Keys order by column, then x, then row within the column.
+static_assert(kBrick == 2, "kKeyOrder is written for columns of 2 x 2 rows");
+__constant__ unsigned char kKeyOrder[4][27] = {
+    {0, 1, 2, 4, 8, 5, 9, 6, 10, 16, 32, 17, 33, 18, 34, 20, 24, 36, 40, 21, 25, 37, 41, 22, 26, 38, 42},
+    {0, 4, 1, 5, 2, 6, 8, 9, 10, 16, 20, 32, 36, 17, 21, 33, 37, 18, 22, 34, 38, 24, 40, 25, 41, 26, 42},
+    {0, 16, 1, 17, 2, 18, 4, 8, 20, 24, 5, 9, 21, 25, 6, 10, 22, 26, 32, 33, 34, 36, 40, 37, 41, 38, 42},
+    {0, 4, 16, 20, 1, 5, 17, 21, 2, 6, 18, 22, 8, 24, 9, 25, 10, 26, 32, 36, 33, 37, 34, 38, 40, 41, 42},
+};
+
 template <int BS>
 __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
@@ -329,6 +340,22 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
                 nb++;
             }
         };
+#if MPSG_KEY_ORDER
+        // the 27 cells in ascending key order, so that every list is sorted by slot: the order
+        // depends only on the cell's row within its 2 x 2 column (kKeyOrder[case])
+        const int kc = (cy & 1) | ((cz & 1) << 1);
+#pragma unroll 1
+        for (int t = 0; t < 27; ++t) {
+            const int code = kKeyOrder[kc][t];
+            const int x = cx + (code & 3) - 1, y = cy + ((code >> 2) & 3) - 1, z = cz + (code >> 4) - 1;
+            if (x < 0 || x >= sc.nx || y < 0 || y >= sc.ny || z < 0 || z >= sc.nz) continue;
+            const unsigned long long key = cell_key(sc, x, y, z);
+            uint2 e;
+            if (fluid_cell(d, p.slots, key, e)) scan_range(d.pos, e.x, e.y, fluid_test);
+            const uint2 eb = d.btable[key];
+            if (eb.x < eb.y) scan_range(d.bpos, eb.x, eb.y, bnd_test);
+        }
+#else
         for (int dz = -1; dz <= 1; ++dz) {
             const int z = cz + dz;
             if (z < 0 || z >= sc.nz) continue;
@@ -344,6 +371,7 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
                 }
             }
         }
+#endif
         if (over) atomicOr(&d.ctr->flags, 1);
         nf = min(nf, unsigned(p.cap_f));
         nb = min(nb, unsigned(p.cap_b));
