@@ -4,16 +4,18 @@
 //                          (src/MPS_Object/MPSSpatialHash.cu:53-77, .cuh:83-145); new scheme:
 //                          clamped floor cells, 64-bit keys, stable radix sort, SoA reorder.
 //   k_build_nbrs           BuildNeighorhood x3 (MPSSpatialHash.cu:142-218, .cuh:147-271);
-//                          one pass over 9 cell rows instead of count+scan+fill.
+//                          one pass over the 27 cells in key order instead of count+scan+fill.
 //   k_bvolume              ComputeBoundaryParticleVolume* (MPSSPHBaseUtil.cuh:10-86)
 //   k_density_alpha        ComputeDensity*, DensityColorTest, ComputeDFSPHFactor*, ResetForce,
 //                          ApplyGravity, UpdateVelocity (MPSSystem.cpp:240-255) fused.
 //   k_pressure_A / _B      ComputeDensityDelta* + Compute{DF,CD}Stiffness + residual
 //                          (MPSSPHDFSPHUtil.cuh:139-340) / ApplyDFSPH* + UpdateVelocity
-//                          (:342-468); loop control of MPSSPHDFSPHUtil.cu:270-441 on the device.
+//                          (:342-468); loop control of MPSSPHDFSPHUtil.cu:270-441 on the device
+//                          (k_pressure_decide between the two passes).
 //   k_st_factor, k_cg_*    ComputeSurfaceTensionFactor/CGb/CGAp, ComputeCGViscosityAp,
 //                          ComputeFinalCGAp (MPSSPHNonPressureUtil.cuh:425-648) and CGSolver
-//                          (MPSSolver.cuh:12-73, MPSCGKernel.cuh:5-133) with device-side dots.
+//                          (MPSSolver.cuh:12-73, MPSCGKernel.cuh:5-133) with device-side dots
+//                          (k_cg_decide3 / k_cg_beta3 / k_cg_decide2: the solver's scalars).
 //   k_advect               BoundaryCollision + UpdatePosition (MPSAdvectUtil.cuh:36-77).
 #include "mps_internal.cuh"
 
