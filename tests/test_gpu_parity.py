@@ -216,16 +216,19 @@ def test_reference_scene_step(mps, orc):
     assert rel_err(p[:, :3], o.get("pos")) < 1e-4
 
 
-def test_batched_equals_single(mps):
+@pytest.mark.parametrize("form", [0, 1])
+def test_batched_equals_single(mps, form):
+    """Scenes stepped in one batch equal the same scenes stepped alone, bit for bit, in both CG
+    arrangements."""
     from mps_cuda_gb300 import BatchedSimulation, Simulation, scenes
     scs = scenes.batched_scenes(4, seed=3, nmin=500, nmax=3000)
-    b = BatchedSimulation(scs)
+    b = BatchedSimulation(scs, cg_form=form)
     b.step(2)
     pb, vb = b.get_fluid()
     its = b.scene_iters()
     off = 0
     for k, sc in enumerate(scs):
-        s = Simulation.from_scene(sc)
+        s = Simulation.from_scene(sc, cg_form=form)
         s.step(2)
         p, v = s.get_fluid()
         assert np.array_equal(p, pb[off:off + sc.n]) and np.array_equal(v, vb[off:off + sc.n]), k
