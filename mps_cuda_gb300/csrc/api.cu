@@ -81,7 +81,7 @@ void mps_handle::release() {
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol,
-                     (void**)&partial, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
+                     (void**)&partial, (void**)&acc, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
                      (void**)&keys, (void**)&keys_tmp, (void**)&vals, (void**)&vals_tmp, (void**)&sort_counts,
                      (void**)&stage_pos, (void**)&stage_vel};
     for (void** q : ptrs) {
@@ -180,6 +180,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.bpos = h->bpos;
     d.bvol = h->bvol;
     d.partial = h->partial;
+    d.acc = h->acc;
     d.solve = h->solve;
     d.ctr = h->ctr;
     d.scene_iters = h->scene_iters;
@@ -297,6 +298,11 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->bpos, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->bvol, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->partial, 2 * (S / 64 + 1)));
+    // the loop-sum accumulators start at zero; each decide kernel zeroes what it has read (one
+    // region more than the scenes: the profiling forms of the pass kernels add into it, unread)
+    const size_t acc_words = (size_t(h->nscenes) + 1) * kAccLanes * kAccStride;
+    MPS_CUDA_TRY(dalloc(&h->acc, acc_words));
+    MPS_CUDA_TRY(cudaMemset(h->acc, 0, acc_words * sizeof(unsigned long long)));
     MPS_CUDA_TRY(dalloc(&h->solve, size_t(h->nscenes)));
     MPS_CUDA_TRY(cudaMemset(h->solve, 0, size_t(h->nscenes) * sizeof(SceneSolve)));
     MPS_CUDA_TRY(dalloc(&h->ctr, 1));

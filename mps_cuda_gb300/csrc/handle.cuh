@@ -54,6 +54,7 @@ struct mps_handle {
     float4* bpos = nullptr;
     float* bvol = nullptr;
     double* partial = nullptr;
+    unsigned long long* acc = nullptr;
     mpsg::SceneSolve* solve = nullptr;
     mpsg::StepCounters* ctr = nullptr;
     int* scene_iters = nullptr;

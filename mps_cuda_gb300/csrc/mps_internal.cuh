@@ -100,6 +100,14 @@ struct Params {
     double df_tol_d, cd_tol_d, cg_tol_d;
 };
 
+// Loop-sum accumulators (sph.cu): lanes a scene, and 64-bit words a lane (one 128-byte line;
+// eight are used, four for each of two components).
+#ifndef MPSG_ACC_LANES
+#define MPSG_ACC_LANES 128
+#endif
+constexpr int kAccLanes = MPSG_ACC_LANES;   // a multiple of 32
+constexpr int kAccStride = 16;
+
 // Device pointers of one step (buffer a is read, buffer b written by the reorder).
 struct Dev {
     float4 *pos, *vel;            // current (sorted) state
@@ -130,7 +138,8 @@ struct Dev {
     unsigned char* tape_adv;      // adjoint recording: collision branch per slot (2 bits per axis)
     const float4* bpos;           // boundary (x, y, z, h)
     float* bvol;
-    double* partial;              // per-block FP64 partial sums (2 per block)
+    double* partial;              // per-block partial sums of the CG operator pass and the Jacobi sweep
+    unsigned long long* acc;      // loop-sum accumulators: (scenes + 1) x kAccLanes x kAccStride words
     SceneSolve* solve;
     StepCounters* ctr;
     int* scene_iters;             // 3 per scene (DF, CG, CD) of the last step

@@ -108,6 +108,119 @@ __device__ __forceinline__ void put_partial(const Dev& d, int b, double v0, doub
     reinterpret_cast<float4*>(d.partial)[b] = make_float4(a.x, a.y, c.x, c.y);
 }
 
+// Loop sums through per-scene integer accumulators (pressure pass A, the two-pass CG operator and
+// the three-pass CG update; the three-pass CG operator keeps its per-block partials, below).
+// Each warp of a pass kernel adds its FP32 sum, scaled by 2^64 and truncated to an integer, as
+// three signed 42-bit limbs (bits 0-41, 42-83, 84-125) into one lane of its scene's accumulator;
+// a non-finite sum or one of magnitude 2^62 or more counts in a fourth word and makes the scene
+// sum NaN.  Integer adds are exact, so a scene sum does not depend on the order in which warps
+// finish nor on how the scene is cut into blocks, and the decide kernel after the pass reads the
+// lanes with one warp instead of summing a partial per block.  Limb sums stay below 2^63 for up
+// to 2^21 additions a lane.  Layout: one 128-byte line a lane,
+// acc[(scene * kAccLanes + lane) * kAccStride + 4 * component + word]; region `nscenes` takes the
+// additions of the profiling forms, which no decide kernel reads.  1M dam break, same box:
+// 6.409 ms a step with per-block partials everywhere, 6.344 ms with accumulators everywhere
+// (the CG operator pass 112.8 -> 118.9 us: its warps end on two components' atomics), 6.272 ms
+// with this split (CG update 20.9 -> 19.6 us, the decide kernels after these passes one warp).
+__device__ __forceinline__ unsigned long long* acc_at(const Dev& d, int s) {
+    return d.acc + size_t(s) * (kAccLanes * kAccStride);
+}
+constexpr unsigned long long kLimbMask = (1ull << 42) - 1ull;
+// Called by every thread of a pass block: each warp sums its threads' values (NC components) in
+// FP32 (a butterfly, so every lane holds the sums), and lanes 4c + k add word k of component c to
+// accumulator lane (warp index in the grid % kAccLanes) of scene s, or of the unread region when
+// prof is set.  Word k < 3 is limb k of floor(|v| 2^64) for the warp sum v, from its FP32 bits
+// (v = m 2^(e - 150) with the 24-bit significand m and biased exponent e, so |v| 2^64 =
+// m 2^(e - 86)), negated for v < 0; word 3 counts sums that are infinite, NaN or 2^62 or more.
+// Warps add their own sums and retire independently: an FP64 block sum split into limbs by one
+// thread lengthened the end of every block (operator pass +10 us at 1M with integer shifts, more
+// with FP64 steps), and a shared-memory merge of the warps' limbs with one set of atomics a block
+// was no faster than this.
+template <int NC>
+__device__ __forceinline__ void warp_acc_put(const Dev& d, const Params& p, int s, bool prof, float a, float b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(kFull, a, o);
+        if (NC == 2) b += __shfl_xor_sync(kFull, b, o);
+    }
+    const int lane = threadIdx.x & 31;
+    if (lane >= 4 * NC) return;
+    const int k = lane & 3;
+    const unsigned bits = __float_as_uint(lane < 4 ? a : b);
+    const unsigned e = (bits >> 23) & 0xffu;
+    const bool bad = e >= 189u;   // |v| >= 2^62, infinity or NaN
+    unsigned long long w;
+    if (k == 3) {
+        w = bad ? 1ull : 0ull;
+    } else {
+        const unsigned long long m = e ? ((bits & 0x7fffffu) | 0x800000u) : 0u;   // subnormal: below 2^-64
+        const int t = int(e) - 86 - 42 * k;   // limb k holds bits [42 k, 42 k + 42) of m 2^(e - 86)
+        const unsigned long long l = bad ? 0ull : t >= 0 ? (t < 42 ? (m << t) & kLimbMask : 0ull)
+                                                         : (t > -24 ? m >> (-t) : 0ull);
+        w = (bits >> 31) ? 0ull - l : l;
+    }
+    if (w) {
+        const unsigned wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        unsigned long long* g = acc_at(d, prof ? p.nscenes : s) + size_t(wid & (kAccLanes - 1)) * kAccStride;
+        atomicAdd(g + 4 * (lane >> 2) + k, w);
+    }
+}
+// Moves the carries up so that limbs 0 and 1 lie in [0, 2^42) (arithmetic shifts: floor division).
+__device__ __forceinline__ void limb_carry(long long& l0, long long& l1, long long& l2) {
+    long long cy = l0 >> 42;
+    l0 -= cy * (1ll << 42);
+    l1 += cy;
+    cy = l1 >> 42;
+    l1 -= cy * (1ll << 42);
+    l2 += cy;
+}
+// Run by one full warp: the sum of scene s's component c, which it then zeroes for the next pass.
+// The limbs are summed and normalised in integers to the magnitude of the sum (all three
+// non-negative), so the only roundings are the two additions of the final FP64 sum, which add
+// terms of one sign, the same on every run.
+__device__ __forceinline__ double acc_take(const Dev& d, int s, int c) {
+    constexpr int U = kAccLanes / 32;
+    const int lane = threadIdx.x & 31;
+    unsigned long long* a = acc_at(d, s) + 4 * c;
+    ulonglong2 q[U][2];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const ulonglong2* w = reinterpret_cast<const ulonglong2*>(a + (lane + 32 * u) * kAccStride);
+        q[u][0] = __ldcg(w);
+        q[u][1] = __ldcg(w + 1);
+    }
+    long long l0 = 0, l1 = 0, l2 = 0;
+    unsigned long long bad = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        ulonglong2* w = reinterpret_cast<ulonglong2*>(a + (lane + 32 * u) * kAccStride);
+        w[0] = make_ulonglong2(0ull, 0ull);
+        w[1] = make_ulonglong2(0ull, 0ull);
+        l0 += static_cast<long long>(q[u][0].x);
+        l1 += static_cast<long long>(q[u][0].y);
+        l2 += static_cast<long long>(q[u][1].x);
+        bad += q[u][1].y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        l0 += __shfl_xor_sync(kFull, l0, o);
+        l1 += __shfl_xor_sync(kFull, l1, o);
+        l2 += __shfl_xor_sync(kFull, l2, o);
+        bad += __shfl_xor_sync(kFull, bad, o);
+    }
+    if (bad) return __longlong_as_double(0x7ff8000000000000ll);
+    limb_carry(l0, l1, l2);
+    const bool neg = l2 < 0;   // limbs 0 and 1 are non-negative now, so the sign is limb 2's
+    if (neg) {
+        l0 = -l0;
+        l1 = -l1;
+        l2 = -l2;
+        limb_carry(l0, l1, l2);
+    }
+    const double r = double(l2) * 0x1p20 + (double(l1) * 0x1p-22 + double(l0) * 0x1p-64);
+    return neg ? -r : r;
+}
+
 // Deterministic sum of this scene's per-block partials (component c of 2), run by one block of
 // NT threads over blocks of SPB slots.
 template <int NT, int SPB>
@@ -122,15 +235,14 @@ __device__ double scene_partial_sum(const Dev& d, const Scene& sc, int c, double
     return block_sum<NT>(v, sh);
 }
 
-// Deterministic sums of scene sc's per-block partials (both components; blocks of spb slots) by one
-// block of NT threads: kSumILP loads in flight per thread, combined in a fixed order.
 #ifndef MPSG_DECIDE_NT
 #define MPSG_DECIDE_NT 1024
 #endif
 #ifndef MPSG_SUM_ILP
 #define MPSG_SUM_ILP 4
 #endif
-constexpr int kDecideThreads = MPSG_DECIDE_NT;
+constexpr int kAccDecideThreads = 32;   // one warp reads a scene's accumulator lanes
+constexpr int kDecideThreads = MPSG_DECIDE_NT;   // a decide kernel over per-block partials
 constexpr int kSumILP = MPSG_SUM_ILP;
 // Deterministic sums of scene sc's per-block partials (blocks of spb slots; component 0, or both
 // when NC = 2) by one block of NT threads: kSumILP loads in flight per thread, combined in a fixed
@@ -517,7 +629,6 @@ __global__ void k_set_cond(Dev d, unsigned long long cond) {
 // mode 1: constant density, kappa = rho/rho0 + dt delta - 1 (MPSSPHDFSPHUtil.cuh:259-340).
 template <int BS>
 __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, unsigned long long cond, int use_cond) {
-    __shared__ double2 sh2[BS / 32];
     const int i = blockIdx.x * BS + threadIdx.x;
     // the slot's own data loads before the scene and solver-state lookups (the grid covers exactly
     // the allocated slots; padding slots have no neighbours)
@@ -571,21 +682,19 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         d.delta[i] = delta;
         if (d.tape_code) d.tape_code[i] = code;
     }
-    const double2 bs2 = block_sum2_f<BS>(err, 0.0f, sh2);
-    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, 0.0);
+    warp_acc_put<1>(d, p, s, use_cond == 2, err, 0.0f);
 }
 
-// Loop decision of a DF/CD pass (MPSSPHDFSPHUtil.cu:404-433), one block per scene after
-// k_pressure_A: the scene's per-block partials (blocks of bs slots) summed in a fixed order, the
-// mean error, the break rule, the iteration counter; the last scene to decide sets the loop
-// condition.  Deciding in the pass's own last block cost every block a fence and a ticket and
-// left the GPU idle during the last block's sum (about 17 us of a 1M CG operator pass); here the
-// pass kernel's blocks only write their partials.  A stopped scene's do_update is cleared here: a
+// Loop decision of a DF/CD pass (MPSSPHDFSPHUtil.cu:404-433), one warp per scene after
+// k_pressure_A: the scene's error sum from its accumulator, the mean error, the break rule, the
+// iteration counter; the last scene to decide sets the loop condition.  Deciding in the pass's
+// own last block cost every block a fence and a ticket and left the GPU idle during the last
+// block's sum (about 17 us of a 1M CG operator pass); here the pass kernel's warps only add their
+// sums.  A stopped scene's do_update is cleared here: a
 // scene that reached its cap stopped with its last update still to run, and the passes after it
 // in the same loop body must not repeat that update.
-__global__ void __launch_bounds__(kDecideThreads) k_pressure_decide(Dev d, Params p, int mode, int bs,
+__global__ void __launch_bounds__(kAccDecideThreads) k_pressure_decide(Dev d, Params p, int mode, int bs,
                                                                     unsigned long long cond, int use_cond) {
-    __shared__ double2 sh[32];
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
     if (!S.active) {
@@ -593,7 +702,8 @@ __global__ void __launch_bounds__(kDecideThreads) k_pressure_decide(Dev d, Param
         return;
     }
     const Scene& sc = d.scenes[s];
-    const double tot = scene_partials<kDecideThreads, 1>(d, sc, bs, sh).x;
+    (void)bs;
+    const double tot = acc_take(d, s, 0);
     if (threadIdx.x == 0) {
         const double mean = tot / double(sc.n);
         const int l = S.iter;
@@ -841,7 +951,6 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
 // r.r < tol and loop counter (MPSSolver.cuh:33-60); r0 = b - A x0 comes from k_cg_b.
 template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long long cond, int use_cond) {
-    __shared__ double2 sh2[BS / 32];
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
     const Scene& sc = d.scenes[s];
@@ -854,16 +963,14 @@ __global__ void __launch_bounds__(BS) k_cg_ap(Dev d, Params p, unsigned long lon
         rr = r.x * r.x + r.y * r.y + r.z * r.z;
         rw = r.x * w.x + r.y * w.y + r.z * w.z;
     }
-    const double2 bs2 = block_sum2_f<BS>(rr, rw, sh2);
-    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, bs2.y);
+    warp_acc_put<2>(d, p, s, use_cond == 2, rr, rw);
 }
 
-// The two-pass CG's decision after k_cg_ap (one block per scene, as k_cg_decide3): r.r and r.w,
+// The two-pass CG's decision after k_cg_ap (one warp per scene, from the accumulator): r.r and r.w,
 // the stop test, beta = (r.r) / (r.r)_old and alpha = (r.r) / (r.w - beta (r.r) / alpha_old)
 // (first iteration: beta = 0, alpha = (r.r) / (r.w)).
-__global__ void __launch_bounds__(kDecideThreads) k_cg_decide2(Dev d, Params p, int bs, unsigned long long cond,
+__global__ void __launch_bounds__(kAccDecideThreads) k_cg_decide2(Dev d, Params p, int bs, unsigned long long cond,
                                                                int use_cond) {
-    __shared__ double2 sh[32];
     pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
@@ -871,7 +978,8 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide2(Dev d, Params p, 
         if (threadIdx.x == 0) S.do_update = 0;
         return;
     }
-    const double2 t = scene_partials<kDecideThreads, 2>(d, d.scenes[s], bs, sh);
+    (void)bs;
+    const double2 t = make_double2(acc_take(d, s, 0), acc_take(d, s, 1));
     const double trr = t.x, trw = t.y;
     if (threadIdx.x == 0) {
         const int l = S.iter;
@@ -949,9 +1057,9 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
     if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, bs2.y);
 }
 
-// The three-pass CG's decision after k_cg_ap3 (one block per scene, as k_pressure_decide): r.r
-// and p.Ap from the partials, the stop test r.r < tol, alpha = r.r / p.Ap, the loop counter
-// (MPSSolver.cuh:33-60).
+// The three-pass CG's decision after k_cg_ap3 (one 1024-thread block per scene): r.r and p.Ap
+// from the operator pass's per-block partials, the stop test r.r < tol, alpha = r.r / p.Ap, the
+// loop counter (MPSSolver.cuh:33-60).
 __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, int bs, unsigned long long cond,
                                                                int use_cond) {
     __shared__ double2 sh[32];
@@ -986,8 +1094,8 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, 
 
 // The three-pass CG's vector passes cover kVecSlots slots per block with NT threads (kVecSlots / NT
 // slots a thread, their loads issued before any store), which keeps more independent loads in
-// flight per thread than one slot a thread.  Blocks keep the 256-slot scene chunks, so the
-// per-block partials and the last-block sum are laid out as for the neighbour kernels.
+// flight per thread than one slot a thread.  Blocks keep the 256-slot scene chunks, so a block
+// belongs to one scene.
 constexpr int kVecSlots = 256;
 #ifndef MPSG_VEC_PDL
 #define MPSG_VEC_PDL 1
@@ -1002,7 +1110,6 @@ constexpr int kVecSlots = 256;
 template <int NT>
 __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile) {
     constexpr int U = kVecSlots / NT;
-    __shared__ double2 sh2[NT / 32];
     // the grid covers exactly the allocated slots, so the data loads go out before the scene and
     // solver-state lookups (padding slots are loaded and not used)
     const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
@@ -1029,19 +1136,17 @@ __global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile)
             rr += r[u].x * r[u].x + r[u].y * r[u].y + r[u].z * r[u].z;
         }
     }
-    const double2 bs2 = block_sum2_f<NT>(rr, 0.0f, sh2);
-    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, 0.0);
+    warp_acc_put<1>(d, p, s, profile != 0, rr, 0.0f);
 }
 
-// beta = (r.r)_new / (r.r)_old from k_cg_update3's partials (blocks of kVecSlots slots), one block
-// per scene that is updating.
-__global__ void __launch_bounds__(kDecideThreads) k_cg_beta3(Dev d) {
-    __shared__ double2 sh[32];
+// beta = (r.r)_new / (r.r)_old from k_cg_update3's sums (the scene's accumulator), one warp per
+// scene that is updating.
+__global__ void __launch_bounds__(kAccDecideThreads) k_cg_beta3(Dev d) {
     pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
     if (!S.do_update) return;
-    const double t = scene_partials<kDecideThreads, 1>(d, d.scenes[s], kVecSlots, sh).x;
+    const double t = acc_take(d, s, 0);
     if (threadIdx.x == 0) S.cg_beta = t / S.rr;
 }
 
@@ -1272,7 +1377,7 @@ void launch_set_cond(const Dev& d, unsigned long long cond, cudaStream_t s) {
 void launch_pressure_A(const Dev& d, const Params& p, int mode, int bs, unsigned long long cond, int use_cond,
                        cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_pressure_A, d, p, mode, cond, use_cond);
-    if (use_cond != 2) k_pressure_decide<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, mode, bs, cond, use_cond);
+    if (use_cond != 2) k_pressure_decide<<<p.nscenes, kAccDecideThreads, 0, s>>>(d, p, mode, bs, cond, use_cond);
 }
 void launch_pressure_B(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                        cudaStream_t s) {
@@ -1292,11 +1397,10 @@ void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 }
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
-    if (use_cond != 2) k_cg_decide2<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, bs, cond, use_cond);
+    if (use_cond != 2) k_cg_decide2<<<p.nscenes, kAccDecideThreads, 0, s>>>(d, p, bs, cond, use_cond);
 }
 // The CG's vector passes stream their arrays; they run with 256-thread blocks whatever the
-// neighbour passes use (half the per-block partials for the residual sums; scenes are padded to
-// 256 slots, so a block still belongs to one scene).
+// neighbour passes use (scenes are padded to 256 slots, so a block still belongs to one scene).
 void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                       cudaStream_t s) {
     (void)bs;
@@ -1313,7 +1417,7 @@ void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 #else
     k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0);
 #endif
-    k_cg_beta3<<<p.nscenes, kDecideThreads, 0, s>>>(d);
+    k_cg_beta3<<<p.nscenes, kAccDecideThreads, 0, s>>>(d);
 }
 void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
     k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 1);
