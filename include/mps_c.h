@@ -81,7 +81,10 @@ typedef struct mps_config {
     int32_t volume_accumulate;   /* 1: reproduce the un-reset boundary volume (MPSSystem.cpp:237-238) */
     int32_t use_graph;           /* 1: whole step as one CUDA graph with device-side loops */
     int32_t block_size;          /* threads per block of the neighbour-sum kernels (64..256) */
-    int32_t stage;               /* reserved, 0 (was: shared-memory staging of the pressure pass; removed, it was slower) */
+    int32_t stage;               /* 0 (default): the CG operator gathers neighbour data from global memory;
+                                    1: the three-pass CG operator gathers from a shared-memory tile of each
+                                    block's distinct neighbours (built once per step: 16-bit ranks, 2 bytes
+                                    a neighbour slot and 20 bytes a particle more memory); not yet timed */
     int32_t sort_digit_bits;     /* radix digit width of the cell sort (1..8) */
     int32_t visc_solver;         /* mps_visc_solver: implicit viscosity/surface-tension solve */
     int32_t cg_form;             /* mps_cg_form: arrangement of the CG iteration (same iterates) */

@@ -81,7 +81,7 @@ void mps_handle::release() {
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol,
-                     (void**)&partial, (void**)&acc, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
+                     (void**)&partial, (void**)&acc, (void**)&nbr_t, (void**)&tile_j, (void**)&tile_n, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
                      (void**)&keys, (void**)&keys_tmp, (void**)&vals, (void**)&vals_tmp, (void**)&sort_counts,
                      (void**)&stage_pos, (void**)&stage_vel};
     for (void** q : ptrs) {
@@ -133,6 +133,7 @@ Params make_params(const mps_handle* h) {
     p.cg_max_iter = c.cg_max_iter;
     p.visc_solver = c.visc_solver == MPS_VISC_JACOBI ? 1 : 0;
     p.cg_form = c.cg_form == MPS_CG_TWO_PASS ? 1 : 0;
+    p.stage = c.stage == 1 ? 1 : 0;
     p.df_tol = float(c.df_tol);
     p.cd_tol = float(c.cd_tol);
     p.cg_tol = float(c.cg_tol);
@@ -181,6 +182,9 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.bvol = h->bvol;
     d.partial = h->partial;
     d.acc = h->acc;
+    d.nbr_t = h->nbr_t;
+    d.tile_j = h->tile_j;
+    d.tile_n = h->tile_n;
     d.solve = h->solve;
     d.ctr = h->ctr;
     d.scene_iters = h->scene_iters;
@@ -303,6 +307,12 @@ int allocate(mps_handle* h) {
     const size_t acc_words = (size_t(h->nscenes) + 1) * kAccLanes * kAccStride;
     MPS_CUDA_TRY(dalloc(&h->acc, acc_words));
     MPS_CUDA_TRY(cudaMemset(h->acc, 0, acc_words * sizeof(unsigned long long)));
+    if (h->cfg.stage == 1) {   // neighbourhood tiles of the CG operator (kTilePerSlot records a slot)
+        MPS_CUDA_TRY(dalloc(&h->nbr_t, S * size_t(h->cfg.max_fluid_neighbors)));
+        MPS_CUDA_TRY(dalloc(&h->tile_j, size_t(kTilePerSlot) * S));
+        MPS_CUDA_TRY(dalloc(&h->tile_n, S / 64 + 1));
+        MPS_CUDA_TRY(cudaMemset(h->tile_n, 0xff, (S / 64 + 1) * sizeof(int)));
+    }
     MPS_CUDA_TRY(dalloc(&h->solve, size_t(h->nscenes)));
     MPS_CUDA_TRY(cudaMemset(h->solve, 0, size_t(h->nscenes) * sizeof(SceneSolve)));
     MPS_CUDA_TRY(dalloc(&h->ctr, 1));
@@ -784,7 +794,7 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;
     if (h->cfg.visc_solver != MPS_VISC_JACOBI) h->cfg.visc_solver = MPS_VISC_CG;
     if (h->cfg.cg_form != MPS_CG_TWO_PASS) h->cfg.cg_form = MPS_CG_THREE_PASS;
-    h->cfg.stage = 0;  // reserved
+    if (h->cfg.stage != 1) h->cfg.stage = 0;
     *out = h;
     return MPS_OK;
 }
@@ -1015,6 +1025,7 @@ int mps_get_stats(mps_handle* h, mps_stats* out, void* stream) {
     if (c.flags & 1) return fail(MPS_E_OVERFLOW, "neighbour list capacity exceeded");
     if (c.flags & 2) return fail(MPS_E_NONFINITE, "non-finite particle position");
     if (c.flags & 4) return fail(MPS_E_STATE, "a device solver loop ran past its iteration bound");
+    if (c.flags & 8) return fail(MPS_E_STATE, "a neighbourhood tile rank was out of range");
     return MPS_OK;
 }
 

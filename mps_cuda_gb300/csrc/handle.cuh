@@ -55,6 +55,9 @@ struct mps_handle {
     float* bvol = nullptr;
     double* partial = nullptr;
     unsigned long long* acc = nullptr;
+    unsigned short* nbr_t = nullptr;
+    unsigned int* tile_j = nullptr;
+    int* tile_n = nullptr;
     mpsg::SceneSolve* solve = nullptr;
     mpsg::StepCounters* ctr = nullptr;
     int* scene_iters = nullptr;

@@ -73,7 +73,7 @@ struct StepCounters {
     unsigned int scenes_done;   // scenes whose last block finished this pass
     int nactive;                // scenes active at the start of the pass
     int nactive_next;           // scenes still active after their decision in the current pass
-    int flags;                  // bit0 overflow, bit1 non-finite
+    int flags;                  // bit0 overflow, bit1 non-finite, bit2 loop guard, bit3 tile rank out of range
     int passes;                 // loop bodies run in the current solve (hard guard)
     unsigned long long fluid_pairs, boundary_pairs;
     unsigned long long iters_total[3];  // sum over steps and scenes of the loop counter (DF, CG, CD)
@@ -96,6 +96,7 @@ struct Params {
     int min_iter_df, min_iter_cd, max_iter, cg_max_iter;
     int visc_solver;              // 0 CG, 1 Jacobi
     int cg_form;                  // 0 three-pass (reference), 1 two-pass
+    int stage;                    // 1: the three-pass CG operator gathers from per-block neighbourhood tiles
     float df_tol, cd_tol, cg_tol; // stored as float for the kernel args; compared in FP64
     double df_tol_d, cd_tol_d, cg_tol_d;
 };
@@ -107,6 +108,9 @@ struct Params {
 #endif
 constexpr int kAccLanes = MPSG_ACC_LANES;   // a multiple of 32
 constexpr int kAccStride = 16;
+// Neighbourhood tiles of the CG operator (mps_config.stage = 1): capacity in records per slot of
+// an operator block (a 128-slot block holds up to 640 distinct neighbour slots).
+constexpr int kTilePerSlot = 5;
 
 // Device pointers of one step (buffer a is read, buffer b written by the reorder).
 struct Dev {
@@ -140,6 +144,9 @@ struct Dev {
     float* bvol;
     double* partial;              // per-block partial sums of the CG operator pass and the Jacobi sweep
     unsigned long long* acc;      // loop-sum accumulators: (scenes + 1) x kAccLanes x kAccStride words
+    unsigned short* nbr_t;        // stage 1: tile rank of each fluid neighbour, interleaved like nbr_f
+    unsigned int* tile_j;         // stage 1: per operator block, its distinct neighbour slots (ascending)
+    int* tile_n;                  // stage 1: per operator block, the tile's size, or -1 (global gathers)
     SceneSolve* solve;
     StepCounters* ctr;
     int* scene_iters;             // 3 per scene (DF, CG, CD) of the last step
@@ -242,6 +249,15 @@ __device__ __forceinline__ unsigned ld_stream(const unsigned* p) {
 #if MPSG_STREAM_HINT
     unsigned v;
     asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+#else
+    return *p;
+#endif
+}
+__device__ __forceinline__ unsigned ld_stream(const unsigned short* p) {
+#if MPSG_STREAM_HINT
+    unsigned short v;
+    asm("ld.global.nc.L1::no_allocate.u16 %0, [%1];" : "=h"(v) : "l"(p));
     return v;
 #else
     return *p;

@@ -942,6 +942,157 @@ __device__ __forceinline__ float3 apply_A(const Dev& d, const Params& p, int i, 
     return apply_A(d, p, i, q, factor, d.pos[i], q[i], d.cnt[i]);
 }
 
+// ---- neighbourhood tiles of the CG operator (mps_config.stage = 1)
+// An operator block's pairs reach few distinct slots (1M dam break at rest: 514 on average for a
+// 128-slot block's 3,600 pairs, each used about 7 times), while a warp's gather of them touches
+// about 15 cache lines for 29 lanes.  k_build_tiles lists each block's distinct neighbour slots in
+// ascending order (tile_j) and gives every pair its 16-bit rank in that list (nbr_t); the tiled
+// operator loads the block's positions and directions into shared memory once per pass and
+// gathers from there.  A block with more than kTilePerSlot records a slot keeps the global gathers
+// (tile_n = -1).  Every loop is bounded, and a rank outside the tile is skipped and flagged (bit 3).
+__host__ __device__ constexpr int pow2_at_least(int v) {
+    int r = 1;
+    while (r < v) r <<= 1;
+    return r;
+}
+__host__ __device__ constexpr int log2_exact(int v) {
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+}
+template <int BS>
+__global__ void __launch_bounds__(BS) k_build_tiles(Dev d, Params p) {
+    constexpr int TM = kTilePerSlot * BS;            // tile capacity
+    constexpr int HS = pow2_at_least(2 * TM);         // open-addressing set of the block's slots
+    constexpr int LH = log2_exact(HS);
+    constexpr int PS = pow2_at_least(TM);             // sort width
+    constexpr unsigned kEmpty = 0xffffffffu;
+    __shared__ unsigned set[HS];
+    __shared__ unsigned uniq[PS];
+    __shared__ int s_cnt, s_over, s_k;
+    const int blk = blockIdx.x;
+    const int i = blk * BS + threadIdx.x;
+    for (int t = threadIdx.x; t < HS; t += BS) set[t] = kEmpty;
+    if (threadIdx.x == 0) {
+        s_cnt = 0;
+        s_over = 0;
+        s_k = 0;
+    }
+    __syncthreads();
+    const int s = block_scene(d, BS);
+    const Scene& sc = d.scenes[s];
+    const size_t stride = size_t(p.slots);
+    const bool live = i < sc.slot_begin + sc.n;
+    const int nf = live ? int(d.cnt[i] & 0xffffu) : 0;
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = ld_stream(d.nbr_f + size_t(k) * stride + size_t(i));
+        unsigned h = (j * 0x9E3779B1u) >> (32 - LH);
+        bool placed = false;
+        for (int probe = 0; probe < HS; ++probe) {
+            const unsigned old = atomicCAS(&set[h], kEmpty, j);
+            if (old == kEmpty) {
+                if (atomicAdd(&s_cnt, 1) >= TM) s_over = 1;
+                placed = true;
+                break;
+            }
+            if (old == j) {
+                placed = true;
+                break;
+            }
+            h = (h + 1u) & unsigned(HS - 1);
+        }
+        if (!placed) s_over = 1;
+    }
+    __syncthreads();
+    const int T = s_cnt;
+    if (s_over || T > TM) {   // uniform: shared values after the barrier
+        if (threadIdx.x == 0) d.tile_n[blk] = -1;
+        return;
+    }
+    for (int t = threadIdx.x; t < HS; t += BS) {
+        const unsigned v = set[t];
+        if (v != kEmpty) {
+            const int o = atomicAdd(&s_k, 1);
+            if (o < PS) uniq[o] = v;
+        }
+    }
+    __syncthreads();
+    for (int t = T + int(threadIdx.x); t < PS; t += BS) uniq[t] = kEmpty;
+    __syncthreads();
+    // bitonic sort of uniq[0, PS), ascending
+    for (int size = 2; size <= PS; size <<= 1) {
+        for (int half = size >> 1; half > 0; half >>= 1) {
+            for (int t = threadIdx.x; t < PS / 2; t += BS) {
+                const int lo = 2 * half * (t / half) + (t % half), hi = lo + half;
+                const bool up = (lo & size) == 0;
+                const unsigned a = uniq[lo], b = uniq[hi];
+                if ((a > b) == up) {
+                    uniq[lo] = b;
+                    uniq[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    unsigned* tj = d.tile_j + size_t(blk) * TM;
+    for (int t = threadIdx.x; t < T; t += BS) tj[t] = uniq[t];
+    bool bad = false;
+    for (int k = 0; k < nf; ++k) {
+        const unsigned j = ld_stream(d.nbr_f + size_t(k) * stride + size_t(i));
+        int lo = 0, hi = T;
+        while (lo < hi) {   // at most log2(TM) + 1 rounds
+            const int mid = (lo + hi) >> 1;
+            if (uniq[mid] < j) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo >= T || uniq[lo] != j) bad = true;
+        d.nbr_t[size_t(k) * stride + size_t(i)] = static_cast<unsigned short>(lo < T ? lo : 0);
+    }
+    if (bad) atomicOr(&d.ctr->flags, 8);
+    if (threadIdx.x == 0) d.tile_n[blk] = T;
+}
+
+// apply_A with the neighbours' positions and directions read from the block's tile (tx, tq of T
+// records); the same pairs, order and arithmetic as apply_A.
+__device__ __forceinline__ float3 apply_A_tile(const Dev& d, const Params& p, int i, const float4* tx,
+                                               const float4* tq, int T, float factor, float4 xi, float4 qi,
+                                               unsigned cnt) {
+    constexpr int U = 4;   // stream loads in flight per thread
+    const size_t stride = size_t(p.slots);
+    const int nf = int(cnt & 0xffffu);
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    bool bad = false;
+    for (int k = 0; k < nf; k += U) {
+        unsigned r[U];
+        float2 cf[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool in = k + u < nf;
+            r[u] = in ? ld_stream(d.nbr_t + size_t(k + u) * stride + size_t(i)) : 0u;
+            cf[u] = in ? ld_stream(d.cg_coef + size_t(k + u) * stride + size_t(i)) : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (k + u < nf) {
+                if (r[u] >= unsigned(T)) {
+                    bad = true;
+                } else {
+                    const float4 xj = tx[r[u]], qj = tq[r[u]];
+                    const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+                    const float px = qi.x - qj.x, py = qi.y - qj.y, pz = qi.z - qj.z;
+                    const float t = cf[u].y * (px * dx + py * dy + pz * dz);
+                    sx += cf[u].x * px - t * dx;
+                    sy += cf[u].x * py - t * dy;
+                    sz += cf[u].x * pz - t * dz;
+                }
+            }
+        }
+    }
+    if (bad) atomicOr(&d.ctr->flags, 8);
+    const float f1 = 1.0f + factor;
+    return make_float3(qi.x * f1 + p.dt * sx, qi.y * f1 + p.dt * sy, qi.z * f1 + p.dt * sz);
+}
+
 // Two-pass CG form (cg_form 1): the Chronopoulos-Gear arrangement (the same iterates as the
 // reference's CGSolver in exact arithmetic): per iteration one operator pass w = A r with the
 // dots r.r and r.w, then one vector pass p = r + beta p, s = w + beta s (s = A p),
@@ -1048,6 +1199,48 @@ __global__ void __launch_bounds__(BS) k_cg_ap3(Dev d, Params p, unsigned long lo
         const float4 q = d.cg_p[i];
         const unsigned c = d.cnt[i];
         const float3 a = apply_A(d, p, i, d.cg_p, p.cg_factor, xi, q, c);
+        d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
+        const float4 r = d.cg_r[i];
+        rr = r.x * r.x + r.y * r.y + r.z * r.z;
+        pap = q.x * a.x + q.y * a.y + q.z * a.z;
+    }
+    const double2 bs2 = block_sum2_f<BS>(rr, pap, sh2);
+    if (threadIdx.x == 0) put_partial(d, blockIdx.x, bs2.x, bs2.y);
+}
+
+// k_cg_ap3 with the neighbours' positions and directions gathered from the block's tile
+// (mps_config.stage = 1; a block without a tile uses the global gathers).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_cg_ap3_tile(Dev d, Params p, unsigned long long cond, int use_cond) {
+    constexpr int TM = kTilePerSlot * BS;
+    extern __shared__ float4 tile[];   // TM positions, then TM directions
+    __shared__ double2 sh2[BS / 32];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const int s = block_scene(d, BS);
+    if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
+    const Scene& sc = d.scenes[s];
+    const int T = d.tile_n[blockIdx.x];
+    const bool tiled = T >= 0 && T <= TM;
+    if (tiled) {
+        const unsigned* tj = d.tile_j + size_t(blockIdx.x) * TM;
+        for (int t = threadIdx.x; t < T; t += BS) {
+            const unsigned j = tj[t];
+            if (j < unsigned(p.slots)) {
+                tile[t] = d.pos[j];
+                tile[TM + t] = d.cg_p[j];
+            } else {
+                atomicOr(&d.ctr->flags, 8);
+            }
+        }
+    }
+    __syncthreads();
+    float rr = 0.0f, pap = 0.0f;
+    if (i < sc.slot_begin + sc.n) {
+        const float4 xi = d.pos[i];
+        const float4 q = d.cg_p[i];
+        const unsigned c = d.cnt[i];
+        const float3 a = tiled ? apply_A_tile(d, p, i, tile, tile + TM, T, p.cg_factor, xi, q, c)
+                               : apply_A(d, p, i, d.cg_p, p.cg_factor, xi, q, c);
         d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
         const float4 r = d.cg_r[i];
         rr = r.x * r.x + r.y * r.y + r.z * r.z;
@@ -1394,6 +1587,7 @@ void launch_st_factor(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 }
 void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_b, d, p);
+    if (p.stage == 1 && p.cg_form == 0 && p.visc_solver == 0) MPSG_BS_SWITCH(bs, k_build_tiles, d, p);   // for k_cg_ap3_tile
 }
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
@@ -1407,7 +1601,14 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long 
     launch_after_decide(k_cg_update<256>, p.slots / 256, 256, s, d, p, cond, use_cond, limit);
 }
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_cg_ap3, d, p, cond, use_cond);
+    if (p.stage == 1) {
+        const size_t sm = size_t(2 * kTilePerSlot) * size_t(bs) * sizeof(float4);   // 40 KB at most (256 slots)
+        if (bs == 128) k_cg_ap3_tile<128><<<p.slots / 128, 128, sm, s>>>(d, p, cond, use_cond);
+        else if (bs == 64) k_cg_ap3_tile<64><<<p.slots / 64, 64, sm, s>>>(d, p, cond, use_cond);
+        else k_cg_ap3_tile<256><<<p.slots / 256, 256, sm, s>>>(d, p, cond, use_cond);
+    } else {
+        MPSG_BS_SWITCH(bs, k_cg_ap3, d, p, cond, use_cond);
+    }
     if (use_cond != 2) k_cg_decide3<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, bs, cond, use_cond);
 }
 void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
