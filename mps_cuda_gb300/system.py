@@ -213,6 +213,8 @@ class Simulation:
         # DF finish + solve set-up (ST factor, coefficients + r0, init, condition), solve finish +
         # CD set-up, CD finish + advect
         static += 5 + 4 + 2
+        if self.cfg.stage == 1 and not jacobi and self.cfg.cg_form != L.CG_TWO_PASS:
+            static += 1   # the operator's neighbourhood tiles, built after the coefficients
         # per pass: pressure A + its decision + pressure B; three-pass CG: operator + decision +
         # update + beta + direction; two-pass: operator + decision + update; Jacobi: one sweep
         cg = 1 if jacobi else (3 if self.cfg.cg_form == L.CG_TWO_PASS else 5)
