@@ -48,6 +48,8 @@ def overrides(args) -> dict:
         out["cg_form"] = args.cg_form
     if args.block_size is not None:
         out["block_size"] = args.block_size
+    if getattr(args, "stage", None) is not None:
+        out["stage"] = args.stage
     return out
 
 
@@ -116,17 +118,42 @@ def radix_passes(sim) -> int:
     return math.ceil(bits / 8)
 
 
-def cpu_baseline(scene, max_steps: int = 1):
-    """FP64 OpenMP oracle on the host cores: one full step of the same workload."""
+def workload_config(scene, world: int = 1) -> dict:
+    """The `config` object of both arms' JSON lines (same keys and values for the same workload)."""
+    cfg = scene.config
+    return {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,
+            "kernel": "cubic spline" if cfg.get("kernel", 1) == 1 else "poly6 / spiky",
+            "dt": scene.physics["dt"],
+            "tolerances": "density %g, divergence %g, CG r.r %g" % (cfg.get("cd_tol", 1e-3), cfg.get("df_tol", 1e-3),
+                                                                 cfg.get("cg_tol", 1e-2)),
+            "l2": "inputs larger than L2: state + neighbour lists + CG vectors ~%.0f MB > 129 MB"
+                  % ((scene.n * (32 + 4 * 40 + 80)) / 1e6),
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def cpu_baseline(scene, pos4, vel4, gpu_iters, budget_s: float = 12.0, max_steps: int = 6):
+    """FP64 OpenMP oracle on the host cores, on the GPU's timed window: it starts from the GPU's
+    state at the start of that window (pos4 / vel4 in particle-ID order) and runs whole steps
+    until `budget_s` of CPU time has passed (at least one step)."""
+    import numpy as np
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     o = O.from_scene(scene, threads=threads)
+    o.set_fluid(pos4[:, :3].astype(np.float64), vel4[:, :3].astype(np.float64), vel4[:, 3].astype(np.float64),
+                pos4[:, 3].astype(np.float64))
+    steps, iters = 0, []
     t0 = time.perf_counter()
-    o.step(max_steps)
+    while steps < max_steps and (steps == 0 or time.perf_counter() - t0 < budget_s):
+        o.step(1)
+        st = o.stats()
+        iters.append([st["df_iters"], st["cg_iters"], st["cd_iters"]])
+        steps += 1
     dt = time.perf_counter() - t0
-    return {"value": scene.n * max_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{max_steps} full step(s) of {scene.name} ({scene.n} fluid, {scene.nb} boundary) from the "
-                      f"initial state, FP64 OpenMP restatement of the reference step, {dt:.1f} s"}
+    return {"value": scene.n * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the first {steps} step(s) of the GPU's timed window of {scene.name} ({scene.n} fluid, "
+                      f"{scene.nb} boundary), from the GPU's state at the window's start; FP64 OpenMP restatement "
+                      f"of the reference step on {threads} host threads, {dt:.1f} s",
+            "iterations_per_step": iters, "gpu_iterations_per_step_mean": gpu_iters}
 
 
 def run_ours(args, scene, rank, world, local_rank):
@@ -156,15 +183,26 @@ def run_ours(args, scene, rank, world, local_rank):
     barrier()
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    repeat_ms = []
     with ClockSampler(local_rank) as clk:
         e0.record(stream)
         sim.step(args.steps, stream)
         e1.record(stream)
         e1.synchronize()
+        torch.cuda.synchronize(dev)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        st1 = sim.stats()
+        # further windows of the same length continuing the run (spread of the figure, and more
+        # clock samples under load); `value` is the first window's
+        for _ in range(args.repeats):
+            r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            r0.record(stream)
+            sim.step(args.steps, stream)
+            r1.record(stream)
+            r1.synchronize()
+            repeat_ms.append(r0.elapsed_time(r1) / args.steps)
     torch.cuda.synchronize(dev)
-    barrier()
-    ms = e0.elapsed_time(e1)
-    st1 = sim.stats()
     t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if dist:
         import torch.distributed as td
@@ -228,12 +266,12 @@ def run_ours(args, scene, rank, world, local_rank):
         "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,
-                   "kernel": "cubic spline", "dt": scene.physics["dt"],
-                   "l2": "inputs larger than L2: state + neighbour lists + CG vectors ~%.0f MB > 129 MB"
-                         % ((scene.n * (32 + 4 * 40 + 80)) / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(scene, world),
         "iterations_per_step": {"df": iters[0] / args.steps, "cg": iters[1] / args.steps, "cd": iters[2] / args.steps},
+        "windows": {"ms_per_step": [ms_max / args.steps] + repeat_ms,
+                    "median_ms_per_step": statistics.median([ms_max / args.steps] + repeat_ms),
+                    "note": "the timed window, then %d more windows of %d steps continuing the run" %
+                            (len(repeat_ms), args.steps)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": src, "traffic": traffic, "traffic_source": "profiles/dram_traffic.json (ncu capture at 512k particles scaled to 1M)" if traffic else None,
                      "algorithmic_bytes_per_launch": algo, "ms_per_launch": per[dom],
@@ -246,7 +284,8 @@ def run_ours(args, scene, rank, world, local_rank):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(scene)
+        line["cpu_baseline"] = cpu_baseline(scene, snap_p, snap_v,
+                                            [iters[k] / args.steps for k in range(3)])
     if dist:
         import torch.distributed as td
         td.destroy_process_group()
@@ -708,14 +747,14 @@ def run_reference(args, scene, rank, world, local_rank):
         "impl": "reference", "metric": METRIC if scene.name == "dam_break_1m" else f"particle-steps/s (DFSPH, {scene.name})", "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": scene.name, "fluid_particles": scene.n, "boundary_particles": scene.nb,
-                   "kernel": "cubic spline (USE_CUBIC_KERNEL 1)", "tolerances": "1e-3 / 1e-3",
-                   "implementation": "moonsh5009/MPS_CUDA step, FP64, rebuilt headless for sm_103a",
-                   "l2": "inputs larger than L2"},
+        "config": workload_config(scene, world),
+        "implementation": "moonsh5009/MPS_CUDA step, FP64, rebuilt headless for sm_103a (USE_CUBIC_KERNEL 1, "
+                          "tolerance literals set to the configuration's 1e-3 / 1e-3)",
         "last_step_loops": {"df": loops[0], "cg": loops[1], "cd": loops[2]},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": None, "kind": "reference",
-                         "sample": f"{args.steps} steps of the reference's own CUDA step on the GPU (it has no CPU "
-                                   f"implementation); host wall clock around its synchronous step calls"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "reference",
+                         "sample": f"{args.steps} steps of the reference's own CUDA step on the GPU, driven by one "
+                                   f"host thread (the reference has no CPU implementation of the step); host wall "
+                                   f"clock around its synchronous step calls"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "clocks": clk.summary(),
     }
@@ -744,6 +783,10 @@ def main():
                     help="CG arrangement: 0 three-pass (the reference's, library default), 1 two-pass")
     ap.add_argument("--block-size", type=int, default=None, choices=[64, 128, 256],
                     help="threads per block of the neighbour-sum kernels (library default 128)")
+    ap.add_argument("--stage", type=int, default=None, choices=[0, 1],
+                    help="neighbour passes: 1 = gathers from shared-memory neighbourhood tiles")
+    ap.add_argument("--repeats", type=int, default=4,
+                    help="further timed windows after the first (reported beside value)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.steps is None:

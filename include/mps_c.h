@@ -81,10 +81,11 @@ typedef struct mps_config {
     int32_t volume_accumulate;   /* 1: reproduce the un-reset boundary volume (MPSSystem.cpp:237-238) */
     int32_t use_graph;           /* 1: whole step as one CUDA graph with device-side loops */
     int32_t block_size;          /* threads per block of the neighbour-sum kernels (64..256) */
-    int32_t stage;               /* 0 (default): the CG operator gathers neighbour data from global memory;
-                                    1: the three-pass CG operator gathers from a shared-memory tile of each
-                                    block's distinct neighbours (built once per step: 16-bit ranks, 2 bytes
-                                    a neighbour slot and 20 bytes a particle more memory); not yet timed */
+    int32_t stage;               /* 0 (default): the neighbour passes gather neighbour data from global
+                                    memory; 1: the three-pass CG operator gathers from a shared-memory tile
+                                    of each block's distinct neighbours, built with the neighbour lists
+                                    (16-bit ranks: 2 bytes a neighbour slot and 20 bytes a particle more
+                                    memory) */
     int32_t sort_digit_bits;     /* radix digit width of the cell sort (1..8) */
     int32_t visc_solver;         /* mps_visc_solver: implicit viscosity/surface-tension solve */
     int32_t cg_form;             /* mps_cg_form: arrangement of the CG iteration (same iterates) */
@@ -125,6 +126,8 @@ typedef struct mps_stats {
     int64_t passes_total[3]; /* DF, CG, CD solver passes launched since creation (>= runs_total: a
                               * graph loop body holds several CG passes; the ones after the stop
                               * return at once) */
+    int64_t tile_blocks[2];  /* stage 1: blocks of the last neighbour build with a neighbourhood tile,
+                              * and blocks whose neighbourhood exceeded the tile (global gathers) */
 } mps_stats;
 
 typedef struct mps_handle mps_handle;
@@ -178,7 +181,8 @@ enum mps_phase {
 };
 int mps_phase(mps_handle* h, int32_t phase, void* stream);
 
-/* Per-particle fields by name: "density","alpha","pressure","delta","aux"(2: rho, ST factor),"color"(4),
+/* Per-particle fields by name: "density","alpha","pressure","delta","density_deviation" (rho/rho0 - 1
+ * from the compensated density sums, which the stiffness reads),"aux"(2: rho, ST factor),"color"(4),
  * "pos"(4),"vel"(4),"ids"(u32),"bvol"(boundary),"bpos"(boundary, 4),
  * "nbr_count"(u32: fluid + boundary * 65536),"cell_key"(u64),"cg_b"(4),"cg_x"(4).
  * order: 0 = current slot order (sorted by cell), 1 = particle ID order.
@@ -213,7 +217,8 @@ int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream
  * float4 x,y,z,w; w unused) on the grid (origin, cell, dims) and stable-sorts them: keys_out[k]
  * is the k-th smallest key, order_out[k] the index of that particle.  Scratch lives in one fixed
  * device array inside the library (about 3.1 MB, held by every GPU that loads it until exit);
- * n > MPS_NOALLOC_MAX_PARTICLES returns MPS_E_INVALID.  The first call on a device looks up that
+ * n > MPS_NOALLOC_MAX_PARTICLES returns MPS_E_INVALID, and so does pos4 not 16-byte aligned
+ * (keys_out and order_out need 8- and 4-byte alignment).  The first call on a device looks up that
  * array with the device current: make it before any stream capture.  Calls that overlap on the
  * GPU share the array and race; serialise them. */
 #define MPS_NOALLOC_MAX_PARTICLES 262144
@@ -222,6 +227,69 @@ int mps_cell_sort_noalloc(const float* pos4, int64_t n, const float origin[3], f
 
 /* Cell grid of the step (one scene): origin, cell size, dims. */
 int mps_get_grid(mps_handle* h, float origin[3], float* cell, int32_t dims[3]);
+
+/* ---- Function-granular calls (the building blocks of the C++ drop-in API, mps_reference.hpp) ----
+ * One call per function of the reference's step API that mps::System::OnUpdate calls
+ * (MPSSystem.cpp:220-278), for single-scene handles.  The step fuses some of them into one kernel;
+ * each op here runs alone with the same arithmetic, so a frame driven op by op (with mps_phase for
+ * the hash, lists and solver drivers) gives the same bits as mps_step.
+ *   MPS_OP_DENSITY_SUB    ComputeDensitySub (MPSSPHBaseUtil.h:19-31): names the neighbour set
+ *                         (`parts`: MPS_PART_FLUID, MPS_PART_BOUNDARY) of the next DENSITY_FINAL
+ *   MPS_OP_DENSITY_FINAL  ComputeDensityFinal (:32-34): one pass over the named sets (Kahan sums)
+ *   MPS_OP_COLOR          DensityColorTest (:35-37)
+ *   MPS_OP_FACTOR_SUB / MPS_OP_FACTOR_FINAL  ComputeDFSPHFactorSub / Final (MPSSPHDFSPHUtil.h:10-25)
+ *   MPS_OP_GRAVITY        ApplyGravity (MPSAdvectUtil.h:16): names gravity for the next UPDATE_VELOCITY
+ *   MPS_OP_UPDATE_VELOCITY UpdateVelocity (:17): v += dt g where m > 1e-10
+ *   MPS_OP_COLLISION      BoundaryCollision (:19)
+ *   MPS_OP_POSITION       UpdatePosition (:18); completes the frame (the step counter advances)
+ *   MPS_OP_ST_FACTOR      ComputeSurfaceTensionFactor (MPSSPHNonPressureUtil.h:34-37)
+ * A Final without its Sub calls returns MPS_E_STATE. */
+enum mps_op_id {
+    MPS_OP_DENSITY_SUB = 0,
+    MPS_OP_DENSITY_FINAL = 1,
+    MPS_OP_COLOR = 2,
+    MPS_OP_FACTOR_SUB = 3,
+    MPS_OP_FACTOR_FINAL = 4,
+    MPS_OP_GRAVITY = 5,
+    MPS_OP_UPDATE_VELOCITY = 6,
+    MPS_OP_COLLISION = 7,
+    MPS_OP_POSITION = 8,
+    MPS_OP_ST_FACTOR = 9
+};
+#define MPS_PART_FLUID 1
+#define MPS_PART_BOUNDARY 2
+int mps_op(mps_handle* h, int32_t op, int32_t parts, void* stream);
+
+/* Device addresses of the library's per-particle arrays, in the current slot order (cell-sorted;
+ * slot k holds particle ids[k]; arrays are padded to `slots`).  The fluid's position and velocity
+ * arrays alternate between two buffers at every cell sort (MPS_PHASE_SORT / mps_step): views
+ * taken before a sort name the previous order.  Neighbour lists are interleaved: the k-th
+ * neighbour slot of slot i is at nbr_*[k * nbr_stride + i]; nbr_count[i] = fluid count | boundary
+ * count << 16. */
+typedef struct mps_device_views {
+    int64_t n, nb, slots;
+    float* pos4;          /* (x, y, z, support radius h = 4 r) */
+    float* vel4;          /* (vx, vy, vz, mass) */
+    uint32_t* ids;
+    float* density;
+    float* pressure;      /* stiffness kappa of the last solver iteration */
+    float* alpha;         /* DFSPH factor */
+    float* delta;         /* density change rate of the last pressure iteration */
+    float* color4;
+    float* scratch4;      /* 4 floats a slot of scratch (overwritten by the viscosity solve) */
+    float* bpos4;         /* boundary (x, y, z, h), cell-sorted at set time */
+    float* bvol;
+    uint32_t* nbr_fluid;
+    uint32_t* nbr_boundary;
+    uint32_t* nbr_count;
+    int64_t nbr_stride;
+    int32_t cap_fluid, cap_boundary;
+    int32_t volume_accumulate;
+} mps_device_views;
+int mps_get_device_views(mps_handle* h, mps_device_views* out);
+
+/* cudaMemsetAsync of a device range to zero (ResetREAL of the drop-in API). */
+int mps_device_zero(void* dev_ptr, int64_t bytes, void* stream);
 
 /* ---- Batched scenes (many independent scenes, one set of launches per pass) ---- */
 /* Scenes are concatenated: fluid of scene s is particles [fluid_offsets[s], fluid_offsets[s+1])

@@ -3,142 +3,42 @@
 // moonsh5009/MPS_CUDA drives its step through mps::System (src/MPS_System/MPSSystem.h:24-76) with
 // an SPH model made of an SPHObject, an SPHMaterial (src/MPS_Object/MPSSPHMaterial.h:9-45) and a
 // SpatialHash, a boundary ObstacleModel sampled from a mesh, and PhysicsParam
-// (src/MPS_Object/MPSUniformDef.h:19-25).  This header keeps those names, fields and setter
-// semantics so that a caller of the reference moves over with few edits:
-//   - mps::PhysicsParam {dt, gravity, min, max} and mps::SPHMaterialParam (same fields);
-//   - mps::SPHMaterial: the constructor's defaults and SetParam / SetRadius / SetViscosity /
-//     SetXSPH / SetSurfaceTension / SetColor (MPSSPHMaterial.cpp:4-44);
-//   - mps::System: SetDevice, OnUpdate (one frame of MPSSystem.cpp:191-291, skipped while the
-//     simulation is paused as b_runSim does), the frame counter; the scene set-up that the
-//     reference hard-codes in Initalize / *TestScene is passed in (SetPhysics, SetMaterial,
-//     SetFluid, SetBoundary, SampleBoundaryMesh);
-//   - mps::kernel::*: the frame's phases under the names of the functions OnUpdate calls.
-// Differences: errors throw mps::Error (the reference reports nothing); state lives in the
-// library and is read back with GetFluid / GetField instead of GL-mapped buffers.
+// (src/MPS_Object/MPSUniformDef.h:19-25).  mps::System here owns one library handle and the
+// reference-shaped models over it (mps_reference.hpp: SPHModel, ObstacleModel, GBArchiver), so that
+// the reference's OnUpdate body runs against it with its call sequence unchanged
+// (m_pSPHModel, m_pBoundaryModel, m_pGBArchiver, m_frame, b_runSim), and adds:
+//   - scene set-up that the reference hard-codes in Initalize / *TestScene, passed in instead
+//     (SetPhysics, SetMaterial, SetFluid, SetBoundary, SampleBoundaryMesh);
+//   - OnUpdate as one graph-launched frame (mps_step), the fast path;
+//   - GetFluid / GetField to read the state back (the reference reads GL-mapped buffers).
+// Errors throw mps::Error (the reference reports nothing).
 #pragma once
 
-#include <array>
 #include <cstdint>
-#include <stdexcept>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "mps_c.h"
+#include "mps_reference.hpp"
 
 namespace mps {
-
-using REAL = double;
-using REAL3 = std::array<REAL, 3>;
-
-class Error : public std::runtime_error {
-public:
-    Error(int code, const std::string& what) : std::runtime_error(what), m_code(code) {}
-    int code() const { return m_code; }
-
-private:
-    int m_code;
-};
-
-inline void Check(int code) {
-    if (code != MPS_OK) {
-        const char* m = mps_last_error();
-        throw Error(code, m ? m : "mps error");
-    }
-}
-
-// PhysicsParam (MPSUniformDef.h:19-25).
-struct PhysicsParam {
-    REAL dt = 0.005;
-    REAL3 gravity{0.0, -9.8, 0.0};
-    REAL3 min{-5.0, -5.0, -5.0};
-    REAL3 max{5.0, 5.0, 5.0};
-};
-
-// SPHMaterialParam (MPSSPHMaterial.h:9-21).
-struct SPHMaterialParam {
-    REAL radius;
-    REAL mass;
-    REAL density;
-    REAL volume;
-    REAL viscosity;
-    REAL XSPH;
-    REAL surfaceTension;
-    std::array<float, 4> color;
-};
-
-// SPHMaterial (MPSSPHMaterial.cpp): radius is the support radius h (the reference calls
-// SetRadius(4 r)); V = h^3 / 48 * 3.141592 and m = density * V as the reference computes them.
-class SPHMaterial {
-public:
-    SPHMaterial() {
-        SetParam(0.01, 1.0);
-        SetViscosity(0.025);
-        SetXSPH(0.1);
-        SetSurfaceTension(100.0);
-        SetColor({0.3f, 0.8f, 0.2f, 1.0f});
-    }
-    void SetParam(REAL radius, REAL density) {
-        m_param.radius = radius;
-        m_param.volume = radius * radius * radius / 48.0 * 3.141592;
-        m_param.density = density;
-        m_param.mass = density * m_param.volume;
-    }
-    void SetRadius(REAL radius) { SetParam(radius, GetDensity()); }
-    void SetViscosity(REAL viscosity) { m_param.viscosity = viscosity; }
-    void SetXSPH(REAL XSPH) { m_param.XSPH = XSPH; }
-    void SetSurfaceTension(REAL surfaceTension) { m_param.surfaceTension = surfaceTension; }
-    void SetColor(const std::array<float, 4>& color) { m_param.color = color; }
-
-    REAL GetRadius() const { return m_param.radius; }
-    REAL GetMass() const { return m_param.mass; }
-    REAL GetDensity() const { return m_param.density; }
-    REAL GetVolume() const { return m_param.volume; }
-    REAL GetViscosity() const { return m_param.viscosity; }
-    REAL GetXSPH() const { return m_param.XSPH; }
-    REAL GetSurfaceTension() const { return m_param.surfaceTension; }
-    const std::array<float, 4>& GetColor() const { return m_param.color; }
-    const SPHMaterialParam& GetParam() const { return m_param; }
-    // A material with explicit mass and volume (physical units, V = spacing^3).
-    void SetPhysical(REAL radius, REAL density, REAL volume) {
-        m_param.radius = radius;
-        m_param.density = density;
-        m_param.volume = volume;
-        m_param.mass = density * volume;
-    }
-
-private:
-    SPHMaterialParam m_param{};
-};
-
-inline mps_material ToC(const SPHMaterialParam& m) {
-    mps_material c{};
-    c.radius = m.radius;
-    c.mass = m.mass;
-    c.density = m.density;
-    c.volume = m.volume;
-    c.viscosity = m.viscosity;
-    c.xsph = m.XSPH;
-    c.surface_tension = m.surfaceTension;
-    return c;
-}
-
-inline mps_physics ToC(const PhysicsParam& p) {
-    mps_physics c{};
-    c.dt = p.dt;
-    for (int k = 0; k < 3; ++k) {
-        c.gravity[k] = p.gravity[size_t(k)];
-        c.min[k] = p.min[size_t(k)];
-        c.max[k] = p.max[size_t(k)];
-    }
-    return c;
-}
 
 // The step of mps::System on one GPU.
 class System {
 public:
-    System() { mps_default_config(&m_config); }
-    ~System() {
-        if (m_h) mps_destroy(m_h);
+    System() {
+        mps_default_config(&m_config);
+        m_pGBArchiver = std::make_unique<GBArchiver>();
+        m_pGBArchiver->m_physicsParam = m_physics;
+    }
+    virtual ~System() {
+        m_pSPHModel.reset();
+        m_pBoundaryModel.reset();
+        if (m_h) {
+            detail::Forget(m_h);
+            mps_destroy(m_h);
+        }
     }
     System(const System&) = delete;
     System& operator=(const System&) = delete;
@@ -147,6 +47,7 @@ public:
     mps_config& Config() { return m_config; }   // before Initalize
     void SetPhysics(const PhysicsParam& p) {
         m_physics = p;
+        m_pGBArchiver->m_physicsParam = p;
         if (m_h) {
             const mps_physics c = ToC(p);
             Check(mps_set_physics(m_h, &c));
@@ -154,25 +55,37 @@ public:
     }
     void SetMaterial(const SPHMaterial& m) {
         m_material = m;
+        if (m_pSPHModel) static_cast<SPHMaterial*>(m_pSPHModel->GetMaterial())->GetParam() = m.GetParam();
         if (m_h) {
             const mps_material c = ToC(m.GetParam());
             Check(mps_set_material(m_h, &c));
         }
     }
-    // Creates the simulation (the part of System::Initalize that is not rendering).
+    // Creates the simulation and its models (the part of System::Initalize that is not rendering):
+    // an SPHModel (SPHObject, SPHMaterial, SpatialHash) and an ObstacleModel (MeshObject,
+    // BoundaryParticleObject, MeshMaterial, SpatialHash), bound to one library handle.
     void Initalize() {
         if (m_h) return;
         const mps_material mat = ToC(m_material.GetParam());
         const mps_physics phys = ToC(m_physics);
         Check(mps_create(&mat, &phys, &m_config, m_device, &m_h));
+        auto sph = std::make_unique<SPHObject>();
+        sph->Bind(m_h);
+        auto sphMat = std::make_unique<SPHMaterial>(m_material);
+        m_pSPHModel = std::make_unique<SPHModel>(std::move(sph), std::move(sphMat), std::make_unique<SpatialHash>());
+        auto bp = std::make_unique<BoundaryParticleObject>();
+        bp->Bind(m_h);
+        m_pBoundaryModel = std::make_unique<ObstacleModel>(std::make_unique<MeshObject>(), std::move(bp),
+                                                           std::make_unique<MeshMaterial>(),
+                                                           std::make_unique<SpatialHash>());
     }
     // Boundary particles: positions (x, y, z) and particle radii; volumes computed on the device.
-    void SetBoundary(const std::vector<REAL>& pos3, const std::vector<REAL>& radius) {
+    void SetBoundary(const std::vector<double>& pos3, const std::vector<double>& radius) {
         Initalize();
         Check(mps_set_boundary(m_h, int64_t(radius.size()), pos3.data(), radius.data(), nullptr));
     }
     // Boundary particles sampled on a triangle mesh (MeshObject::LoadMesh + ParticleSampling).
-    size_t SampleBoundaryMesh(const std::string& obj_path, const REAL3& center, const REAL3& size, REAL mesh_radius) {
+    size_t SampleBoundaryMesh(const std::string& obj_path, const Vec3d& center, const Vec3d& size, double mesh_radius) {
         int64_t nv = 0, nf = 0;
         Check(mps_mesh_load_obj(obj_path.c_str(), center.data(), size.data(), &nv, &nf, nullptr, nullptr));
         std::vector<double> v(size_t(nv) * 3);
@@ -183,17 +96,20 @@ public:
         std::vector<float> p4(size_t(n) * 4);
         const int64_t n2 = mps_mesh_sample(v.data(), nv, f.data(), nf, mesh_radius, p4.data(), nullptr);
         if (n2 != n) Check(n2 < 0 ? int(n2) : MPS_E_STATE);
-        std::vector<REAL> pos3(static_cast<size_t>(n) * 3), rad(static_cast<size_t>(n));
+        std::vector<double> pos3(static_cast<size_t>(n) * 3), rad(static_cast<size_t>(n));
         for (size_t i = 0; i < size_t(n); ++i) {
             for (int k = 0; k < 3; ++k) pos3[3 * i + size_t(k)] = p4[4 * i + size_t(k)];
             rad[i] = p4[4 * i + 3];
         }
         SetBoundary(pos3, rad);
+        auto* mesh = m_pBoundaryModel->GetTarget<MeshObject>();
+        mesh->m_vertices = v;
+        mesh->m_faces = f;
         return size_t(n);
     }
-    // Fluid particles as the reference stores them (REAL3 pos / vel, REAL mass and radius).
-    void SetFluid(const std::vector<REAL>& pos3, const std::vector<REAL>& vel3, const std::vector<REAL>& mass,
-                  const std::vector<REAL>& radius) {
+    // Fluid particles as the reference stores them (xyz position / velocity, mass and radius, FP64).
+    void SetFluid(const std::vector<double>& pos3, const std::vector<double>& vel3, const std::vector<double>& mass,
+                  const std::vector<double>& radius) {
         Initalize();
         Check(mps_set_fluid(m_h, int64_t(mass.size()), pos3.data(), vel3.data(), mass.data(), radius.data(), nullptr));
     }
@@ -242,48 +158,20 @@ public:
         if (phase == MPS_PHASE_ADVECT) m_frame++;
     }
 
+protected:
+    // the reference's members that its OnUpdate body reads (MPSSystem.h:60-72)
+    std::unique_ptr<SPHModel> m_pSPHModel;
+    std::unique_ptr<ObstacleModel> m_pBoundaryModel;
+    std::unique_ptr<GBArchiver> m_pGBArchiver;
+    bool b_runSim = true;
+    uint64_t m_frame = 0;
+
 private:
     mps_handle* m_h = nullptr;
     int m_device = 0;
     mps_config m_config{};
     PhysicsParam m_physics{};
     SPHMaterial m_material{};
-    bool b_runSim = true;
-    uint64_t m_frame = 0;
 };
-
-// The frame's phases under the names of the reference's functions that OnUpdate calls
-// (MPSSystem.cpp:220-278), so that its call sequence can be kept.  Each runs on all of the
-// System's particles; several reference calls map to one phase, as noted.
-namespace kernel {
-// SpatialHash::UpdateHash + ZSort (MPSSpatialHash.cu:53-140): cell keys, sort, reorder.
-inline void UpdateHash(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_SORT, stream); }
-// SpatialHash::BuildNeighorhood, fluid-fluid and fluid-boundary (MPSSpatialHash.cu:142-218).
-inline void BuildNeighorhood(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_NEIGHBORS, stream); }
-namespace SPH {
-// ComputeBoundaryParticleVolumeSub/Final (MPSSPHBaseUtil.cu:9-53); a no-op unless the config
-// asks for the reference's accumulating volume (the static boundary's volume is set once).
-inline void ComputeBoundaryParticleVolume(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_BVOLUME, stream); }
-// ComputeDensitySub/Final + DensityColorTest + ComputeDFSPHFactorSub/Final, then ResetForce /
-// ApplyGravity / UpdateVelocity (MPSSystem.cpp:240-255): one fused pass.
-inline void ComputeDensityAndDFSPHFactor(System& sys, void* stream = nullptr) {
-    sys.Phase(MPS_PHASE_DENSITY_ALPHA, stream);
-}
-// ComputeDFSPHDivergenceFree (MPSSPHDFSPHUtil.h:80-87).
-inline void ComputeDFSPHDivergenceFree(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_DF, stream); }
-// ApplyImplicitViscosityNSurfaceTension (MPSSPHNonPressureUtil.h:61-65).
-inline void ApplyImplicitViscosityNSurfaceTension(System& sys, void* stream = nullptr) {
-    sys.Phase(MPS_PHASE_VISCST, stream);
-}
-// ComputeDFSPHConstantDensity (MPSSPHDFSPHUtil.h:72-79).
-inline void ComputeDFSPHConstantDensity(System& sys, void* stream = nullptr) { sys.Phase(MPS_PHASE_CD, stream); }
-}  // namespace SPH
-namespace Advect {
-// BoundaryCollision + UpdatePosition (MPSAdvectUtil.h:17-19); completes the frame.
-inline void BoundaryCollisionAndUpdatePosition(System& sys, void* stream = nullptr) {
-    sys.Phase(MPS_PHASE_ADVECT, stream);
-}
-}  // namespace Advect
-}  // namespace kernel
 
 }  // namespace mps

@@ -58,7 +58,7 @@ class Stats(C.Structure):
     _fields_ = [("df_iters", C.c_int32), ("cg_iters", C.c_int32), ("cd_iters", C.c_int32), ("flags", C.c_int32),
                 ("df_err", C.c_double), ("cd_err", C.c_double), ("cg_rr", C.c_double), ("fluid_pairs", C.c_int64),
                 ("boundary_pairs", C.c_int64), ("steps", C.c_int64), ("iters_total", C.c_int64 * 3),
-                ("runs_total", C.c_int64 * 3), ("passes_total", C.c_int64 * 3)]
+                ("runs_total", C.c_int64 * 3), ("passes_total", C.c_int64 * 3), ("tile_blocks", C.c_int64 * 2)]
 
 
 EXPORTS = {
@@ -104,6 +104,9 @@ EXPORTS = {
                                        C.c_void_p]),
     "mps_adjoint_memory": (C.c_int64, [C.c_void_p, C.c_int32, C.c_int32]),
     "mps_adjoint_reserve": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "mps_op": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "mps_get_device_views": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mps_device_zero": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
 }
 
 _lib = None

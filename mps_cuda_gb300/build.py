@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 # Extra nvcc flags (e.g. -DMPSG_B_AP=8 to retune a neighbour loop); a change needs build(force=True).
 NVCC_FLAGS += os.environ.get("MPS_GB300_NVCC_FLAGS", "").split()
-SOURCES = ["sort.cu", "sph.cu", "api.cu", "noalloc.cu", "mesh.cu", "adjoint.cu", "scene.cpp"]
+SOURCES = ["sort.cu", "sph.cu", "api.cu", "ops.cu", "noalloc.cu", "mesh.cu", "adjoint.cu", "scene.cpp"]
 
 
 def nvcc() -> str:
@@ -44,7 +44,9 @@ def _compile(src: str, verbose: bool) -> Path:
     out = BUILD / (src + ".o")
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", "-c", str(CSRC / src), "-o", str(out)]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "c++", *NVCC_FLAGS, f"-I{INCLUDE}", "-c", str(CSRC / src), "-o", str(out)]
+        # host code: no floating-point contraction, so x86 and Arm give the same bits
+        cmd = [nvcc(), "-x", "c++", *NVCC_FLAGS, "-Xcompiler", "-ffp-contract=off", f"-I{INCLUDE}", "-c",
+               str(CSRC / src), "-o", str(out)]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -393,7 +393,7 @@ int phase_sort(mps_handle* h, cudaStream_t s) {
 
 void phase_neighbors(mps_handle* h, cudaStream_t s) {
     const Params p = make_params(h);
-    cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 2 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 4 * sizeof(unsigned long long), s);
     launch_build_nbrs(make_dev(h, h->cur), p, block_size(h), s);
 }
 
@@ -553,7 +553,7 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         launch_keys(d, p, c.s);
         MPS_CAP_TRY(radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, h->cfg.sort_digit_bits, c.s));
         launch_reorder(d, p, int(h->n), c.s);
-        MPS_CAP_TRY(cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 2 * sizeof(unsigned long long), c.s));
+        MPS_CAP_TRY(cudaMemsetAsync(&h->ctr->fluid_pairs, 0, 4 * sizeof(unsigned long long), c.s));
         launch_build_nbrs(d, p, bs, c.s);
         if (h->cfg.volume_accumulate) launch_bvolume(d, p, int(h->nb), 1, c.s);
         launch_density_alpha(d, p, bs, c.s);
@@ -679,6 +679,7 @@ bool field_info(mps_handle* h, const std::string& n, FieldInfo& f) {
     else if (n == "alpha") f = {h->alpha, 4, 1, false};
     else if (n == "pressure") f = {h->kappa, 4, 1, false};
     else if (n == "delta") f = {h->delta, 4, 1, false};
+    else if (n == "density_deviation") f = {h->rdev, 4, 1, false};
     else if (n == "aux") f = {h->aux, 4, 2, false};
     else if (n == "color") f = {h->color, 4, 4, false};
     else if (n == "pos") f = {h->pos[c], 4, 4, false};
@@ -1016,6 +1017,8 @@ int mps_get_stats(mps_handle* h, mps_stats* out, void* stream) {
     out->flags = c.flags;
     out->fluid_pairs = int64_t(c.fluid_pairs);
     out->boundary_pairs = int64_t(c.boundary_pairs);
+    out->tile_blocks[0] = int64_t(c.tile_blocks[0]);
+    out->tile_blocks[1] = int64_t(c.tile_blocks[1]);
     out->steps = h->steps;
     for (int k = 0; k < 3; ++k) {
         out->iters_total[k] = int64_t(c.iters_total[k]);

@@ -33,6 +33,10 @@ struct mps_handle {
     bool layout_ready = false;
     int cur = 0;                         // state buffer holding the current order
     int64_t steps = 0;
+    // drop-in API (ops.cu): neighbour sets named by the *Sub calls since the last *Final, and
+    // gravity named by ApplyGravity since the last UpdateVelocity
+    int pending_density = 0, pending_alpha = 0;
+    bool pending_gravity = false;
 
     // device memory
     float4* pos[2] = {nullptr, nullptr};

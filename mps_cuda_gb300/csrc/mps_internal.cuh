@@ -76,6 +76,7 @@ struct StepCounters {
     int flags;                  // bit0 overflow, bit1 non-finite, bit2 loop guard, bit3 tile rank out of range
     int passes;                 // loop bodies run in the current solve (hard guard)
     unsigned long long fluid_pairs, boundary_pairs;
+    unsigned long long tile_blocks[2];  // neighbourhood tiles of the step: blocks with a tile, blocks without
     unsigned long long iters_total[3];  // sum over steps and scenes of the loop counter (DF, CG, CD)
     unsigned long long runs_total[3];   // solver passes that ran (one per iteration; max over scenes)
     unsigned long long passes_total[3]; // solver passes launched (a graph body holds MPSG_CG_UNROLL CG passes)
@@ -381,6 +382,9 @@ void launch_reorder(const Dev& d, const Params& p, int n_real, cudaStream_t s);
 void launch_build_nbrs(const Dev& d, const Params& p, int bs, cudaStream_t s);
 void launch_bvolume(const Dev& d, const Params& p, int nb, int accumulate, cudaStream_t s);
 void launch_density_alpha(const Dev& d, const Params& p, int bs, cudaStream_t s);
+// One part of the fused density pass (what: 1 density, 2 colour, 4 alpha, 8 gravity) over the
+// neighbour sets in `parts` (1 fluid, 2 boundary); returns -1 for an unknown part.
+int launch_density_part(const Dev& d, const Params& p, int bs, int what, int parts, cudaStream_t s);
 void launch_solver_init(const Dev& d, const Params& p, cudaStream_t s);
 void launch_set_cond(const Dev& d, unsigned long long cond, cudaStream_t s);
 void launch_load_state(const Dev& d, const Params& p, const float4* pos4, const float4* vel4, int n,
@@ -412,6 +416,8 @@ void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long con
                    const float4* src, float4* dst, cudaStream_t s);
 void launch_jacobi_finish(const Dev& d, const Params& p, const float4* src, cudaStream_t s);
 void launch_advect(const Dev& d, const Params& p, cudaStream_t s);
+// what: 1 boundary collision (velocities), 2 position update
+void launch_advect_part(const Dev& d, const Params& p, int what, cudaStream_t s);
 void launch_stats(const Dev& d, const Params& p, cudaStream_t s);
 
 }  // namespace mpsg

@@ -17,6 +17,7 @@
 //    different host threads on the same device) race on it and must be serialised by the caller.
 //    Every byte of scratch that a call reads was written earlier in the same call (the histogram
 //    is fully rewritten each digit pass), so the contents left by a previous call never leak in.
+#include <cstdint>
 #include <mutex>
 
 #include "mps_c.h"
@@ -61,6 +62,10 @@ extern "C" int mps_cell_sort_noalloc(const float* pos4, int64_t n, const float o
     if (n < 0 || n > kMax) return MPS_E_INVALID;  // beyond the fixed scratch: rejected
     if (!origin || !dims || !(cell > 0.0f) || (n > 0 && (!pos4 || !keys_out || !order_out))) return MPS_E_INVALID;
     if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return MPS_E_INVALID;
+    // pos4 is read as float4 (16-byte loads), keys and order with their natural alignment
+    if (reinterpret_cast<uintptr_t>(pos4) % 16 != 0 || reinterpret_cast<uintptr_t>(keys_out) % 8 != 0 ||
+        reinterpret_cast<uintptr_t>(order_out) % 4 != 0)
+        return MPS_E_INVALID;
     const unsigned long long cells = cell_key_count(dims[0], dims[1], dims[2]);
     if (cells > (1ull << 40)) return MPS_E_INVALID;
     int dev = 0;
@@ -84,11 +89,17 @@ extern "C" int mps_cell_sort_noalloc(const float* pos4, int64_t n, const float o
     const float inv = 1.0f / cell;
     auto* keys = reinterpret_cast<unsigned long long*>(keys_out);
     auto* vals = reinterpret_cast<unsigned int*>(order_out);
-    k_noalloc_keys<<<int((n + 255) / 256), 256, 0, s>>>(reinterpret_cast<const float4*>(pos4), int(n), origin[0],
-                                                        origin[1], origin[2], inv, dims[0], dims[1], dims[2], keys,
-                                                        vals);
+    // every launch's own status is checked (cudaLaunchKernelEx here, the same in the radix sort), so an
+    // earlier, unrelated error pending in the calling thread is neither reported nor cleared
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(unsigned((n + 255) / 256));
+    cfg.blockDim = dim3(256u);
+    cfg.stream = s;
+    if (cudaLaunchKernelEx(&cfg, k_noalloc_keys, reinterpret_cast<const float4*>(pos4), int(n), origin[0], origin[1],
+                           origin[2], inv, dims[0], dims[1], dims[2], keys, vals) != cudaSuccess)
+        return MPS_E_CUDA;
     int bits = 1;
     while ((1ull << bits) < cells) bits++;
-    if (radix_sort_pairs(keys, vals, tmp_keys, tmp_vals, counts, int(n), bits, 8, s) != cudaSuccess) return MPS_E_CUDA;
-    return cudaGetLastError() == cudaSuccess ? MPS_OK : MPS_E_CUDA;
+    return radix_sort_pairs(keys, vals, tmp_keys, tmp_vals, counts, int(n), bits, 8, s) == cudaSuccess ? MPS_OK
+                                                                                                       : MPS_E_CUDA;
 }

@@ -144,6 +144,17 @@ size_t radix_counts_size(int n) {
     return size_t(kBins) * size_t(nblocks > 0 ? nblocks : 1) + kBins;
 }
 
+// Launches one kernel and returns that launch's status (cudaLaunchKernelEx reports the launch
+// itself, unlike cudaGetLastError, which would also return an earlier, unrelated error of the thread).
+template <class... KArgs, class... Args>
+static cudaError_t launch_checked(void (*k)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(unsigned(grid));
+    cfg.blockDim = dim3(unsigned(block));
+    cfg.stream = s;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 cudaError_t radix_sort_pairs(unsigned long long* keys, unsigned int* vals, unsigned long long* keys_tmp,
                              unsigned int* vals_tmp, unsigned int* counts, int n, int bits, int digit_bits,
                              cudaStream_t s) {
@@ -153,23 +164,32 @@ cudaError_t radix_sort_pairs(unsigned long long* keys, unsigned int* vals, unsig
     const int passes = (bits + digit_bits - 1) / digit_bits;
     unsigned long long *ka = keys, *kb = keys_tmp;
     unsigned int *va = vals, *vb = vals_tmp;
+    cudaError_t e = cudaSuccess;
     for (int p = 0; p < passes; ++p) {
         const int shift = p * digit_bits;
         const int nb = min(digit_bits, bits - shift);
         const unsigned int mask = (1u << nb) - 1u;
         unsigned int* totals = counts + size_t(kBins) * size_t(nblocks);
-        rs_upsweep<<<nblocks, kThreads, 0, s>>>(ka, n, shift, mask, nblocks, counts);
-        rs_scan_rows<<<kBins / kWarps, kThreads, 0, s>>>(counts, nblocks, totals);
-        rs_scan_digits<<<1, kBins, 0, s>>>(totals);
-        rs_downsweep<<<nblocks, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, mask, nblocks, counts, totals);
+        if ((e = launch_checked(rs_upsweep, nblocks, kThreads, s, (const unsigned long long*)ka, n, shift, mask,
+                                nblocks, counts)) != cudaSuccess)
+            return e;
+        if ((e = launch_checked(rs_scan_rows, kBins / kWarps, kThreads, s, counts, nblocks, totals)) != cudaSuccess)
+            return e;
+        if ((e = launch_checked(rs_scan_digits, 1, kBins, s, totals)) != cudaSuccess) return e;
+        if ((e = launch_checked(rs_downsweep, nblocks, kThreads, s, (const unsigned long long*)ka,
+                                (const unsigned int*)va, kb, vb, n, shift, mask, nblocks,
+                                (const unsigned int*)counts, (const unsigned int*)totals)) != cudaSuccess)
+            return e;
         unsigned long long* tk = ka; ka = kb; kb = tk;
         unsigned int* tv = va; va = vb; vb = tv;
     }
     if (ka != keys) {
-        cudaMemcpyAsync(keys, ka, size_t(n) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(vals, va, size_t(n) * sizeof(unsigned int), cudaMemcpyDeviceToDevice, s);
+        if ((e = cudaMemcpyAsync(keys, ka, size_t(n) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s)) !=
+            cudaSuccess)
+            return e;
+        e = cudaMemcpyAsync(vals, va, size_t(n) * sizeof(unsigned int), cudaMemcpyDeviceToDevice, s);
     }
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace mpsg

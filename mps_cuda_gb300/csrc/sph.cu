@@ -350,6 +350,31 @@ __device__ void loop_guard(const Dev& d, unsigned long long cond, int limit) {
     }
 }
 
+// Pair distance d and 1/d from d^2.  The fast form takes rsqrtf (MUFU, about 2 ulp) and
+// d = d^2 / sqrt(d^2); the exact form correctly rounded sqrt and division (0.5 ulp each), for the
+// passes whose sums are small differences (the density deviation and the density change rate).
+#ifndef MPSG_EXACT_DIST_DENS
+#define MPSG_EXACT_DIST_DENS 1
+#endif
+#ifndef MPSG_EXACT_DIST_PA
+#define MPSG_EXACT_DIST_PA 0
+#endif
+template <int EXACT>
+__device__ __forceinline__ void pair_dist(float d2, float& dist, float& invd) {
+    if (EXACT) {
+        dist = sqrtf(d2);
+        invd = d2 > 0.0f ? 1.0f / dist : 0.0f;
+    } else {
+        invd = safe_rsqrt(d2);
+        dist = d2 * invd;
+    }
+}
+// Compensated (Kahan) sums of the density change rate in pressure pass A: delta is a sum of terms
+// of both signs whose result is small against them, and the stiffness is delta against rho/rho0 - 1.
+#ifndef MPSG_DELTA_KAHAN
+#define MPSG_DELTA_KAHAN 1
+#endif
+
 // ------------------------------------------------------------------ sort / reorder
 __global__ void k_keys(Dev d, Params p) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -536,62 +561,85 @@ __global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
 }
 
 // ------------------------------------------------------------------ density + alpha + gravity
-template <int BS>
-__global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p) {
+// What one launch of k_density_alpha computes: the step fuses all four (W_ALL); the drop-in API
+// of the reference's functions (ComputeDensityFinal, DensityColorTest, ComputeDFSPHFactorFinal,
+// UpdateVelocity after ApplyGravity) runs them one at a time with the same arithmetic, so the
+// results are the same bits.  `parts` selects the neighbour sets of the sums (1 fluid, 2 boundary).
+constexpr int W_DENSITY = 1, W_COLOR = 2, W_ALPHA = 4, W_GRAVITY = 8, W_ALL = 15;
+template <int BS, int WHAT>
+__global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p, int parts) {
     const int i = blockIdx.x * BS + threadIdx.x;
     const Scene& sc = d.scenes[block_scene(d, BS)];
     if (i >= sc.slot_begin + sc.n) return;
-    const size_t stride = size_t(p.slots);
-    const float4 xi = d.pos[i];
-    const float invh = 1.0f / xi.w;
-    const unsigned c = d.cnt[i];
-    const int nf = int(c & 0xffffu), nb = int(c >> 16);
-    Kahan rf, gx, gy, gz, sq;
-    rf.add(p.V * kW(0.0f, invh, p.cubic));
-    visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; }, [&](unsigned j, int) { return d.pos[j]; },
-                          [&](const float4& xj, NoStream, int) {
-        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const float invd = safe_rsqrt(d2);
-        const float dist = d2 * invd;
-        rf.add(p.V * kW(dist, invh, p.cubic));
-        const float g = p.V * kG(dist, invd, invh, p.cubic);
-        const float ax = g * dx, ay = g * dy, az = g * dz;
-        gx.add(ax); gy.add(ay); gz.add(az);
-        sq.add(ax * ax + ay * ay + az * az);
-    });
-    Kahan rb;
-    visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
-                          [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
-                          [&](const float4& xj, NoStream, int) {
-        const float vb = xj.w;
-        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const float invd = safe_rsqrt(d2);
-        const float dist = d2 * invd;
-        rb.add(vb * kW(dist, invh, p.cubic));
-        const float g = vb * kG(dist, invd, invh, p.cubic);
-        gx.add(g * dx); gy.add(g * dy); gz.add(g * dz);
-    });
-    const float rho = (rf.s + rb.s) * p.rho0;
-    d.rho[i] = rho;
-    // rho / rho0 - 1 without the rounding of rho itself: rf.s - 1 is exact (Sterbenz), and the
-    // Kahan sums carry their lost low parts in c (true sum = s - c)
-    d.rdev[i] = __fsub_rn(__fadd_rn(__fsub_rn(rf.s, 1.0f), rb.s), __fadd_rn(rf.c, rb.c));
-    // alpha denominator in FP64: |sum grad|^2 + sum |grad|^2, clamp at 1e-20 (MPSSPHDFSPHUtil.cuh:127-137)
-    const double sx = gx.s, sy = gy.s, sz = gz.s;
-    const double f = double(sq.s) + (sx * sx + sy * sy + sz * sz);
-    d.alpha[i] = f > 1.0e-20 ? float(1.0 / f) : 0.0f;
-    const float ratio = rho * p.inv_rho0;
-    float4 col;
-    col.x = fminf(fmaxf(ratio - 1.0f, 0.0f), 1.0f);
-    col.y = fminf(fmaxf(ratio < 1.0f ? ratio : 1.0f - (ratio - 1.0f), 0.0f), 1.0f);
-    col.z = fminf(fmaxf(1.0f - ratio, 0.0f), 1.0f);
-    col.w = 1.0f;
-    d.color[i] = col;
-    float4 v = d.vel[i];
-    if (v.w > 1.0e-10f) { v.x += p.dt * p.gx; v.y += p.dt * p.gy; v.z += p.dt * p.gz; }
-    d.vel[i] = v;
+    constexpr bool kSums = (WHAT & (W_DENSITY | W_ALPHA)) != 0;
+    float rho = 0.0f;
+    if (kSums) {
+        const size_t stride = size_t(p.slots);
+        const float4 xi = d.pos[i];
+        const float invh = 1.0f / xi.w;
+        const unsigned c = d.cnt[i];
+        const int nf = (parts & 1) ? int(c & 0xffffu) : 0, nb = (parts & 2) ? int(c >> 16) : 0;
+        Kahan rf, gx, gy, gz, sq;
+        if (parts & 1) rf.add(p.V * kW(0.0f, invh, p.cubic));
+        visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; }, [&](unsigned j, int) { return d.pos[j]; },
+                              [&](const float4& xj, NoStream, int) {
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            float dist, invd;
+            pair_dist<MPSG_EXACT_DIST_DENS>(d2, dist, invd);
+            if (WHAT & W_DENSITY) rf.add(p.V * kW(dist, invh, p.cubic));
+            if (WHAT & W_ALPHA) {
+                const float g = p.V * kG(dist, invd, invh, p.cubic);
+                const float ax = g * dx, ay = g * dy, az = g * dz;
+                gx.add(ax); gy.add(ay); gz.add(az);
+                sq.add(ax * ax + ay * ay + az * az);
+            }
+        });
+        Kahan rb;
+        visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+                              [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
+                              [&](const float4& xj, NoStream, int) {
+            const float vb = xj.w;
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            float dist, invd;
+            pair_dist<MPSG_EXACT_DIST_DENS>(d2, dist, invd);
+            if (WHAT & W_DENSITY) rb.add(vb * kW(dist, invh, p.cubic));
+            if (WHAT & W_ALPHA) {
+                const float g = vb * kG(dist, invd, invh, p.cubic);
+                gx.add(g * dx); gy.add(g * dy); gz.add(g * dz);
+            }
+        });
+        if (WHAT & W_DENSITY) {
+            rho = (rf.s + rb.s) * p.rho0;
+            d.rho[i] = rho;
+            // rho / rho0 - 1 without the rounding of rho itself: rf.s - 1 is exact (Sterbenz), and
+            // the Kahan sums carry their lost low parts in c (true sum = s - c)
+            d.rdev[i] = __fsub_rn(__fadd_rn(__fsub_rn(rf.s, 1.0f), rb.s), __fadd_rn(rf.c, rb.c));
+        }
+        if (WHAT & W_ALPHA) {
+            // alpha denominator in FP64: |sum grad|^2 + sum |grad|^2, clamp at 1e-20
+            // (MPSSPHDFSPHUtil.cuh:127-137)
+            const double sx = gx.s, sy = gy.s, sz = gz.s;
+            const double f = double(sq.s) + (sx * sx + sy * sy + sz * sz);
+            d.alpha[i] = f > 1.0e-20 ? float(1.0 / f) : 0.0f;
+        }
+    }
+    if (WHAT & W_COLOR) {
+        if (!(WHAT & W_DENSITY)) rho = d.rho[i];
+        const float ratio = rho * p.inv_rho0;
+        float4 col;
+        col.x = fminf(fmaxf(ratio - 1.0f, 0.0f), 1.0f);
+        col.y = fminf(fmaxf(ratio < 1.0f ? ratio : 1.0f - (ratio - 1.0f), 0.0f), 1.0f);
+        col.z = fminf(fmaxf(1.0f - ratio, 0.0f), 1.0f);
+        col.w = 1.0f;
+        d.color[i] = col;
+    }
+    if (WHAT & W_GRAVITY) {
+        float4 v = d.vel[i];
+        if (v.w > 1.0e-10f) { v.x += p.dt * p.gx; v.y += p.dt * p.gy; v.z += p.dt * p.gz; }
+        d.vel[i] = v;
+    }
 }
 
 // ------------------------------------------------------------------ pressure solves
@@ -643,28 +691,39 @@ __global__ void __launch_bounds__(BS) k_pressure_A(Dev d, Params p, int mode, un
         const size_t stride = size_t(p.slots);
         const float invh = 1.0f / xi.w;
         const int nf = int(c & 0xffffu), nb = int(c >> 16);
-        float df = 0.0f;
+#if MPSG_DELTA_KAHAN
+        Kahan df, db;
+#define MPSG_DELTA_ADD(acc, v) acc.add(v)
+#define MPSG_DELTA_VAL(acc) __fsub_rn(acc.s, acc.c)
+#else
+        float df = 0.0f, db = 0.0f;
+#define MPSG_DELTA_ADD(acc, v) acc += (v)
+#define MPSG_DELTA_VAL(acc) acc
+#endif
         visit_batched<MPSG_B_PA, NoStream, XV, MPSG_PF_PA>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; },
                           [&](unsigned j, int) { return XV{d.pos[j], d.vel[j]}; },
                           [&](const XV& t, NoStream, int) {
             const float4 xj = t.x, vj = t.v;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
-            const float invd = safe_rsqrt(d2);
-            const float g = kG(d2 * invd, invd, invh, p.cubic);
-            df += g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
+            float dist, invd;
+            pair_dist<MPSG_EXACT_DIST_PA>(d2, dist, invd);
+            const float g = kG(dist, invd, invh, p.cubic);
+            MPSG_DELTA_ADD(df, g * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z)));
         });
-        float db = 0.0f;
         visit_batched<MPSG_B_PA, NoStream, float4, MPSG_PF_PA>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
                               [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
                               [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
-            const float invd = safe_rsqrt(d2);
-            const float g = kG(d2 * invd, invd, invh, p.cubic);
-            db += xj.w * g * (dx * vi.x + dy * vi.y + dz * vi.z);
+            float dist, invd;
+            pair_dist<MPSG_EXACT_DIST_PA>(d2, dist, invd);
+            const float g = kG(dist, invd, invh, p.cubic);
+            MPSG_DELTA_ADD(db, xj.w * g * (dx * vi.x + dy * vi.y + dz * vi.z));
         });
-        const float delta = p.V * df + db;
+        const float delta = p.V * MPSG_DELTA_VAL(df) + MPSG_DELTA_VAL(db);
+#undef MPSG_DELTA_ADD
+#undef MPSG_DELTA_VAL
         // rho/rho0 + dt delta - 0.8 (DF) and rho/rho0 + dt delta - 1 (CD) from the density deviation
         const float rd = d.rdev[i];
         const float ka = delta * p.dt;
@@ -984,14 +1043,16 @@ __global__ void __launch_bounds__(BS) k_build_tiles(Dev d, Params p) {
     const size_t stride = size_t(p.slots);
     const bool live = i < sc.slot_begin + sc.n;
     const int nf = live ? int(d.cnt[i] & 0xffffu) : 0;
+    volatile int* over = &s_over;
     for (int k = 0; k < nf; ++k) {
+        if (*over) break;   // the block keeps the global gathers: stop inserting
         const unsigned j = ld_stream(d.nbr_f + size_t(k) * stride + size_t(i));
         unsigned h = (j * 0x9E3779B1u) >> (32 - LH);
         bool placed = false;
-        for (int probe = 0; probe < HS; ++probe) {
+        for (int probe = 0; probe < HS && !*over; ++probe) {
             const unsigned old = atomicCAS(&set[h], kEmpty, j);
             if (old == kEmpty) {
-                if (atomicAdd(&s_cnt, 1) >= TM) s_over = 1;
+                if (atomicAdd(&s_cnt, 1) >= TM) *over = 1;
                 placed = true;
                 break;
             }
@@ -1001,12 +1062,15 @@ __global__ void __launch_bounds__(BS) k_build_tiles(Dev d, Params p) {
             }
             h = (h + 1u) & unsigned(HS - 1);
         }
-        if (!placed) s_over = 1;
+        if (!placed) *over = 1;
     }
     __syncthreads();
     const int T = s_cnt;
     if (s_over || T > TM) {   // uniform: shared values after the barrier
-        if (threadIdx.x == 0) d.tile_n[blk] = -1;
+        if (threadIdx.x == 0) {
+            d.tile_n[blk] = -1;
+            atomicAdd(&d.ctr->tile_blocks[1], 1ull);
+        }
         return;
     }
     for (int t = threadIdx.x; t < HS; t += BS) {
@@ -1049,7 +1113,10 @@ __global__ void __launch_bounds__(BS) k_build_tiles(Dev d, Params p) {
         d.nbr_t[size_t(k) * stride + size_t(i)] = static_cast<unsigned short>(lo < T ? lo : 0);
     }
     if (bad) atomicOr(&d.ctr->flags, 8);
-    if (threadIdx.x == 0) d.tile_n[blk] = T;
+    if (threadIdx.x == 0) {
+        d.tile_n[blk] = T;
+        atomicAdd(&d.ctr->tile_blocks[0], 1ull);
+    }
 }
 
 // apply_A with the neighbours' positions and directions read from the block's tile (tx, tq of T
@@ -1471,6 +1538,9 @@ __device__ __forceinline__ float collide(float pos, float lo, float hi, float v,
     return v;
 }
 
+// BoundaryCollision (WHAT bit 1: the velocity against the box) and UpdatePosition (bit 2:
+// x += dt v), fused in the step, one at a time in the drop-in API (same arithmetic).
+template <int WHAT>
 __global__ void k_advect(Dev d, Params p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.slots) return;
@@ -1478,14 +1548,18 @@ __global__ void k_advect(Dev d, Params p) {
     if (i >= sc.slot_begin + sc.n) return;
     float4 x = d.pos[i];
     float4 v = d.vel[i];
-    unsigned cx, cy, cz;
-    v.x = collide(x.x + v.x * p.dt, sc.bminx, sc.bmaxx, v.x, cx);
-    v.y = collide(x.y + v.y * p.dt, sc.bminy, sc.bmaxy, v.y, cy);
-    v.z = collide(x.z + v.z * p.dt, sc.bminz, sc.bmaxz, v.z, cz);
-    x.x += p.dt * v.x; x.y += p.dt * v.y; x.z += p.dt * v.z;
-    d.pos[i] = x;
-    d.vel[i] = v;
-    if (d.tape_adv) d.tape_adv[i] = (unsigned char)(cx | (cy << 2) | (cz << 4));
+    if (WHAT & 1) {
+        unsigned cx, cy, cz;
+        v.x = collide(x.x + v.x * p.dt, sc.bminx, sc.bmaxx, v.x, cx);
+        v.y = collide(x.y + v.y * p.dt, sc.bminy, sc.bmaxy, v.y, cy);
+        v.z = collide(x.z + v.z * p.dt, sc.bminz, sc.bmaxz, v.z, cz);
+        d.vel[i] = v;
+        if (d.tape_adv) d.tape_adv[i] = (unsigned char)(cx | (cy << 2) | (cz << 4));
+    }
+    if (WHAT & 2) {
+        x.x += p.dt * v.x; x.y += p.dt * v.y; x.z += p.dt * v.z;
+        d.pos[i] = x;
+    }
 }
 
 // Loads a state given in particle-ID order (pos4.w = particle radius) into the slot layout.
@@ -1554,12 +1628,30 @@ void launch_reorder(const Dev& d, const Params& p, int n_real, cudaStream_t s) {
 }
 void launch_build_nbrs(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_build_nbrs, d, p);
+    // neighbourhood tiles of the step's neighbour passes: built from the lists they index, so that
+    // lists and tiles always change together
+    if (p.stage == 1) MPSG_BS_SWITCH(bs, k_build_tiles, d, p);
 }
 void launch_bvolume(const Dev& d, const Params& p, int nb, int accumulate, cudaStream_t s) {
     if (nb > 0) k_bvolume<<<nblocks_for(nb, 256), 256, 0, s>>>(d, p, nb, accumulate);
 }
+#define MPSG_BS_SWITCH_W(bs, KERNEL, W, ...)                                                 \
+    do {                                                                                     \
+        if ((bs) == 128) KERNEL<128, W><<<p.slots / 128, 128, 0, s>>>(__VA_ARGS__);          \
+        else if ((bs) == 64) KERNEL<64, W><<<p.slots / 64, 64, 0, s>>>(__VA_ARGS__);         \
+        else KERNEL<256, W><<<p.slots / 256, 256, 0, s>>>(__VA_ARGS__);                      \
+    } while (0)
 void launch_density_alpha(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-    MPSG_BS_SWITCH(bs, k_density_alpha, d, p);
+    MPSG_BS_SWITCH_W(bs, k_density_alpha, W_ALL, d, p, 3);
+}
+int launch_density_part(const Dev& d, const Params& p, int bs, int what, int parts, cudaStream_t s) {
+    switch (what) {
+        case W_DENSITY: MPSG_BS_SWITCH_W(bs, k_density_alpha, W_DENSITY, d, p, parts); return 0;
+        case W_COLOR: MPSG_BS_SWITCH_W(bs, k_density_alpha, W_COLOR, d, p, parts); return 0;
+        case W_ALPHA: MPSG_BS_SWITCH_W(bs, k_density_alpha, W_ALPHA, d, p, parts); return 0;
+        case W_GRAVITY: MPSG_BS_SWITCH_W(bs, k_density_alpha, W_GRAVITY, d, p, parts); return 0;
+        default: return -1;
+    }
 }
 void launch_solver_init(const Dev& d, const Params& p, cudaStream_t s) {
     k_solver_init<<<1, 256, 0, s>>>(d, p);
@@ -1587,7 +1679,6 @@ void launch_st_factor(const Dev& d, const Params& p, int bs, cudaStream_t s) {
 }
 void launch_cg_b(const Dev& d, const Params& p, int bs, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_b, d, p);
-    if (p.stage == 1 && p.cg_form == 0 && p.visc_solver == 0) MPSG_BS_SWITCH(bs, k_build_tiles, d, p);   // for k_cg_ap3_tile
 }
 void launch_cg_ap(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
     MPSG_BS_SWITCH(bs, k_cg_ap, d, p, cond, use_cond);
@@ -1650,7 +1741,11 @@ void launch_store_state(const Dev& d, const Params& p, float4* pos4, float4* vel
     k_store_state<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p, pos4, vel4);
 }
 void launch_advect(const Dev& d, const Params& p, cudaStream_t s) {
-    k_advect<<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
+    k_advect<3><<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
+}
+void launch_advect_part(const Dev& d, const Params& p, int what, cudaStream_t s) {
+    if (what == 1) k_advect<1><<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
+    else k_advect<2><<<nblocks_for(p.slots, 256), 256, 0, s>>>(d, p);
 }
 
 }  // namespace mpsg

@@ -1,8 +1,9 @@
 """Scene and configuration table.
 
-Scenes are built with the library's deterministic generators (mps_gen_block / mps_gen_box_walls /
-mps_gen_sphere) so that every implementation (this package, the FP64 oracle, the reference's own
-CUDA step) gets bit-identical inputs.
+Scenes are built with deterministic generators (NumPy restatements of the library's mps_gen_block /
+mps_gen_box_walls / mps_gen_sphere, bit-identical to them) so that every implementation (this
+package, the FP64 oracle, the reference's own CUDA step) gets bit-identical inputs, and building a
+scene loads no CUDA library.
 
 - ``reference_surface_tension``: the reference's active scene, mps::System::SurfaceTensionTestScene
   (src/MPS_System/MPSSystem.cpp:552-651) with the constants of System::Initalize (:26-72); its
@@ -58,34 +59,102 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
     return a.ctypes.data_as(C.c_void_p)
 
 
+# ---- generators (host set-up code).  NumPy restatements of the library's C-ABI generators
+# mps_gen_block / mps_gen_box_walls / mps_gen_sphere (csrc/scene.cpp), bit-identical to them (a CPU
+# test compares the two), so that building a scene loads no CUDA library: the reference arm of the
+# benchmark builds its inputs with these and maps only the reference's own step.
+_M64 = (1 << 64) - 1
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser on uint64 arrays (wrapping arithmetic), as in csrc/scene.cpp."""
+    x = x + np.uint64(0x9E3779B97F4A7C15)
+    x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def _uniform01(seed: int, counter: np.ndarray) -> np.ndarray:
+    """Uniform doubles in [0, 1) from (seed, counter): the top 53 bits of splitmix64(seed ^ splitmix64(counter))."""
+    r = _splitmix64(np.uint64(seed & _M64) ^ _splitmix64(counter.astype(np.uint64)))
+    return (r >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
 def gen_block(dims, origin, spacing, radius, mass, jitter, seed):
-    lib = L.load()
+    """Jittered lattice block: particle i = (x, y, z) with x fastest sits at
+    origin + spacing * (index + 1) + jitter * U(-1, 1) per axis (FP64, then rounded to FP32)."""
     nx, ny, nz = (int(d) for d in dims)
+    if nx <= 0 or ny <= 0 or nz <= 0:
+        raise ValueError("bad block dimensions")
     n = nx * ny * nz
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    idx = (x.ravel(), y.ravel(), z.ravel())
+    i = np.arange(n, dtype=np.uint64)
     pos = np.zeros((n, 4), np.float32)
+    for a in range(3):
+        u = _uniform01(int(seed), np.uint64(3) * i + np.uint64(a))
+        j = float(jitter) * (2.0 * u - 1.0)
+        pos[:, a] = (float(origin[a]) + float(spacing) * (idx[a] + 1).astype(np.float64) + j).astype(np.float32)
+    pos[:, 3] = np.float32(radius)
     vel = np.zeros((n, 4), np.float32)
-    o = (C.c_double * 3)(*origin)
-    L.check(lib.mps_gen_block(nx, ny, nz, o, spacing, radius, mass, jitter, seed, _ptr(pos), _ptr(vel)))
+    vel[:, 3] = np.float32(mass)
     return pos, vel
 
 
+def _llround(v: float) -> int:
+    """Round half away from zero (C's llround) for v >= 0."""
+    f = math.floor(v)
+    return int(f) + (1 if v - f >= 0.5 else 0)
+
+
 def gen_walls(lo, hi, spacing, radius, open_mask=0):
-    lib = L.load()
-    clo, chi = (C.c_double * 3)(*lo), (C.c_double * 3)(*hi)
-    n = lib.mps_gen_box_walls(clo, chi, spacing, radius, open_mask, None)
-    if n < 0:
+    """Single-layer box walls: lattice points of the box surface (per-axis spacing stretched so that
+    both faces are hit exactly), point (i, j, k) kept when it lies on a face that is not open
+    (bit 2a: the low face of axis a, bit 2a + 1: the high face)."""
+    if not spacing > 0.0:
         raise ValueError("bad wall arguments")
-    out = np.zeros((n, 4), np.float32)
-    lib.mps_gen_box_walls(clo, chi, spacing, radius, open_mask, _ptr(out))
+    n, step = [], []
+    for a in range(3):
+        ext = float(hi[a]) - float(lo[a])
+        if not ext > 0.0:
+            raise ValueError("bad wall arguments")
+        na = max(2, _llround(ext / float(spacing)) + 1)
+        n.append(na)
+        step.append(ext / float(na - 1))
+    k, j, i = np.meshgrid(np.arange(n[2]), np.arange(n[1]), np.arange(n[0]), indexing="ij")
+    c = (i.ravel(), j.ravel(), k.ravel())
+    on = np.zeros(c[0].shape, bool)
+    for a in range(3):
+        if not open_mask & (1 << (2 * a)):
+            on |= c[a] == 0
+        if not open_mask & (1 << (2 * a + 1)):
+            on |= c[a] == n[a] - 1
+    out = np.zeros((int(on.sum()), 4), np.float32)
+    for a in range(3):
+        ca = c[a][on]
+        v = float(lo[a]) + step[a] * ca.astype(np.float64)
+        out[:, a] = np.where(ca == n[a] - 1, float(hi[a]), v).astype(np.float32)
+    out[:, 3] = np.float32(radius)
     return out
 
 
 def gen_sphere(center, R, spacing, radius):
-    lib = L.load()
-    c = (C.c_double * 3)(*center)
-    n = lib.mps_gen_sphere(c, R, spacing, radius, None)
-    out = np.zeros((n, 4), np.float32)
-    lib.mps_gen_sphere(c, R, spacing, radius, _ptr(out))
+    """Fibonacci lattice on a sphere, about one point per spacing^2 of area (the C library's math
+    functions through Python's math module, so the points equal the C-ABI generator's)."""
+    if not (R > 0.0 and spacing > 0.0):
+        raise ValueError("bad sphere arguments")
+    pi = math.acos(-1.0)
+    count = _llround(4.0 * pi * R * R / (spacing * spacing))
+    out = np.zeros((max(count, 0), 4), np.float32)
+    golden = pi * (3.0 - math.sqrt(5.0))
+    for i in range(count):
+        y = 1.0 - 2.0 * (float(i) + 0.5) / float(count)
+        r = math.sqrt(max(0.0, 1.0 - y * y))
+        th = golden * float(i)
+        out[i, 0] = center[0] + R * r * math.cos(th)
+        out[i, 1] = center[1] + R * y
+        out[i, 2] = center[2] + R * r * math.sin(th)
+    out[:, 3] = np.float32(radius)
     return out
 
 

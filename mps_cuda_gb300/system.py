@@ -20,6 +20,7 @@ from .scenes import Scene
 
 FIELD_DTYPES = {
     "density": (np.float32, 1), "alpha": (np.float32, 1), "pressure": (np.float32, 1), "delta": (np.float32, 1),
+    "density_deviation": (np.float32, 1),
     "aux": (np.float32, 2), "color": (np.float32, 4), "pos": (np.float32, 4), "vel": (np.float32, 4),
     "ids": (np.uint32, 1), "nbr_count": (np.uint32, 1), "cell_key": (np.uint64, 1), "cg_b": (np.float32, 4),
     "cg_x": (np.float32, 4), "bvol": (np.float32, 1), "bpos": (np.float32, 4),
@@ -213,8 +214,8 @@ class Simulation:
         # DF finish + solve set-up (ST factor, coefficients + r0, init, condition), solve finish +
         # CD set-up, CD finish + advect
         static += 5 + 4 + 2
-        if self.cfg.stage == 1 and not jacobi and self.cfg.cg_form != L.CG_TWO_PASS:
-            static += 1   # the operator's neighbourhood tiles, built after the coefficients
+        if self.cfg.stage == 1:
+            static += 1   # the neighbourhood tiles, built with the neighbour lists
         # per pass: pressure A + its decision + pressure B; three-pass CG: operator + decision +
         # update + beta + direction; two-pass: operator + decision + update; Jacobi: one sweep
         cg = 1 if jacobi else (3 if self.cfg.cg_form == L.CG_TWO_PASS else 5)

@@ -1,13 +1,103 @@
 // The small dam break (10^3 fluid particles, r = 0.01, spacing 0.02, walls of a 0.5 m box) driven
 // through the C++ layer the way mps::System drives the reference's step; writes the final fluid
 // state (pos4 then vel4, float32, particle-ID order) to argv[1]; argv[3] = "phases" runs each frame
-// through the mps::kernel phase functions in the reference's OnUpdate order instead of OnUpdate.
+// through the reference's step functions (mps_reference.hpp) in mps::System::OnUpdate's call
+// sequence instead of the graph-launched OnUpdate.
+#include <cuda_runtime.h>
+
 #include <cstdio>
 #include <cstdlib>
+#include <sstream>
 #include <string>
 #include <vector>
 
 #include "mps_system.hpp"
+
+// The body of the reference's mps::System::OnUpdate (src/MPS_System/MPSSystem.cpp:191-291), kept
+// statement for statement on purpose: this program checks that the reference's call sequence
+// compiles and runs against the drop-in API and gives the same frames as the library's own step.
+class ReferenceSystem : public mps::System {
+public:
+    void OnUpdateReference() {
+        if (!b_runSim) return;
+        {
+            cudaDeviceSynchronize();
+            std::stringstream ss;
+            ss << "Frame " << m_frame;
+            MTimer::Start(ss.str());
+        }
+        auto pBoundaryParticleObject = static_cast<mps::BoundaryParticleObject*>(m_pBoundaryModel->GetSubObject());
+        auto pBoundaryParticleMaterial = static_cast<mps::MeshMaterial*>(m_pBoundaryModel->GetMaterial());
+        auto pBoundaryParticleHash = static_cast<mps::SpatialHash*>(
+            m_pBoundaryModel->GetTree(static_cast<uint32_t>(mps::ObstacleTreeIdx::SpatialHash)));
+        auto pSPHObject = m_pSPHModel->GetTarget<mps::SPHObject>();
+        auto pSPHMaterial = static_cast<mps::SPHMaterial*>(m_pSPHModel->GetMaterial());
+        auto pSPHHash = static_cast<mps::SpatialHash*>(m_pSPHModel->GetTree());
+
+        const auto pBoundaryParticleRes = pBoundaryParticleObject->GetDeviceResource<mps::BoundaryParticleResource>();
+        const auto pBoundaryParticleParam = pBoundaryParticleRes->GetBoundaryParticleParam().lock();
+        if (!pBoundaryParticleParam) return;
+        const auto pSPHRes = pSPHObject->GetDeviceResource<mps::SPHResource>();
+        const auto pSPHParam = pSPHRes->GetSPHParam().lock();
+        if (!pSPHParam) return;
+        const auto& physParam = m_pGBArchiver->m_physicsParam;
+
+        if ((m_frame % 50u) == 1u) {
+            pBoundaryParticleHash->ZSort(*pBoundaryParticleParam);
+            pSPHHash->ZSort(*pSPHParam);
+        }
+        pBoundaryParticleHash->UpdateHash(*pBoundaryParticleParam);
+        pSPHHash->UpdateHash(*pSPHParam);
+
+        pBoundaryParticleHash->BuildNeighorhood(*pBoundaryParticleParam);
+        pSPHHash->BuildNeighorhood(*pSPHParam);
+        pSPHHash->BuildNeighorhood(*pSPHParam, *pBoundaryParticleParam, pBoundaryParticleHash);
+
+        const auto neiBP2BP = pBoundaryParticleHash->GetNeighborhood(*pBoundaryParticleParam).value_or(mps::NeiParam{nullptr, nullptr});
+        const auto neiSPH2SPH = pSPHHash->GetNeighborhood(*pSPHParam).value_or(mps::NeiParam{nullptr, nullptr});
+        const auto neiSPH2BP = pSPHHash->GetNeighborhood(*pBoundaryParticleParam).value_or(mps::NeiParam{nullptr, nullptr});
+
+        mps::kernel::SPH::ComputeBoundaryParticleVolumeSub(*pBoundaryParticleParam, neiBP2BP);
+        mps::kernel::SPH::ComputeBoundaryParticleVolumeFinal(*pBoundaryParticleParam);
+
+        mps::kernel::Advect::ResetREAL(pSPHParam->pDensity, pSPHParam->size);
+        mps::kernel::SPH::ComputeDensitySub(pSPHMaterial->GetParam(), *pSPHParam, neiSPH2SPH);
+        mps::kernel::SPH::ComputeDensitySub(*pSPHParam, neiSPH2BP, *pBoundaryParticleParam);
+        mps::kernel::SPH::ComputeDensityFinal(pSPHMaterial->GetParam(), *pSPHParam);
+
+        mps::kernel::SPH::DensityColorTest(pSPHMaterial->GetParam(), *pSPHParam);
+
+        mps::kernel::Advect::ResetREAL(pSPHParam->pFactorDFSPH, pSPHParam->size);
+        mps::kernel::Advect::ResetREAL(reinterpret_cast<REAL*>(pSPHParam->pTempVec3), pSPHParam->size * 3);
+        mps::kernel::SPH::ComputeDFSPHFactorSub(pSPHMaterial->GetParam(), *pSPHParam, neiSPH2SPH);
+        mps::kernel::SPH::ComputeDFSPHFactorSub(*pSPHParam, neiSPH2BP, *pBoundaryParticleParam);
+        mps::kernel::SPH::ComputeDFSPHFactorFinal(*pSPHParam);
+
+        mps::kernel::Advect::ResetForce(*pSPHParam);
+        mps::kernel::Advect::ApplyGravity(physParam, *pSPHParam);
+        mps::kernel::Advect::UpdateVelocity(physParam, *pSPHParam);
+
+        mps::kernel::SPH::ComputeDFSPHDivergenceFree(physParam, pSPHMaterial->GetParam(), *pSPHParam,
+                                                     pBoundaryParticleMaterial->GetParam(), *pBoundaryParticleParam,
+                                                     neiSPH2SPH, neiSPH2BP);
+        mps::kernel::SPH::ApplyImplicitViscosityNSurfaceTension(physParam, pSPHMaterial->GetParam(), *pSPHParam,
+                                                                neiSPH2SPH);
+        mps::kernel::SPH::ComputeDFSPHConstantDensity(physParam, pSPHMaterial->GetParam(), *pSPHParam,
+                                                      pBoundaryParticleMaterial->GetParam(), *pBoundaryParticleParam,
+                                                      neiSPH2SPH, neiSPH2BP);
+
+        mps::kernel::Advect::BoundaryCollision(physParam, *pSPHParam);
+        mps::kernel::Advect::UpdatePosition(physParam, *pSPHParam);
+        {
+            cudaDeviceSynchronize();
+            std::stringstream ss;
+            ss << "Frame " << m_frame;
+            MTimer::End(ss.str());
+            OutputDebugStringA("\n");
+        }
+        m_frame++;
+    }
+};
 
 int main(int argc, char** argv) {
     if (argc < 3) {
@@ -28,7 +118,7 @@ int main(int argc, char** argv) {
         phys.min = {0.0, 0.0, 0.0};
         phys.max = {0.5, 0.5, 0.5};
 
-        mps::System sys;
+        ReferenceSystem sys;
         sys.SetDevice(0);
         mps_config& cfg = sys.Config();
         cfg.kernel = MPS_KERNEL_CUBIC_SPLINE;
@@ -63,15 +153,7 @@ int main(int argc, char** argv) {
                 sys.OnUpdate();
                 continue;
             }
-            // the reference's OnUpdate call sequence (MPSSystem.cpp:220-278), phase by phase
-            mps::kernel::UpdateHash(sys);
-            mps::kernel::BuildNeighorhood(sys);
-            mps::kernel::SPH::ComputeBoundaryParticleVolume(sys);
-            mps::kernel::SPH::ComputeDensityAndDFSPHFactor(sys);
-            mps::kernel::SPH::ComputeDFSPHDivergenceFree(sys);
-            mps::kernel::SPH::ApplyImplicitViscosityNSurfaceTension(sys);
-            mps::kernel::SPH::ComputeDFSPHConstantDensity(sys);
-            mps::kernel::Advect::BoundaryCollisionAndUpdatePosition(sys);
+            sys.OnUpdateReference();
         }
         sys.SetRunning(false);
         sys.OnUpdate();   // paused: no step

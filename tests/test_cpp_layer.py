@@ -1,5 +1,6 @@
 """The C++ layer (include/mps_system.hpp): compiles and links against libmps_gb300.so on the CPU;
 on the GPU the example program's state after 20 frames equals the Python API's bit for bit."""
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -15,8 +16,10 @@ def compile_example(out: Path) -> Path:
     if cxx is None:
         pytest.skip("no C++ compiler")
     lib = ROOT / "mps_cuda_gb300"
-    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
-           str(ROOT / "tests/cpp/system_example.cpp"), f"-L{lib}", "-lmps_gb300", f"-Wl,-rpath,{lib}", "-o", str(out)]
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", f"-I{cuda / 'include'}",
+           str(ROOT / "tests/cpp/system_example.cpp"), f"-L{lib}", "-lmps_gb300", f"-Wl,-rpath,{lib}",
+           f"-L{cuda / 'lib64'}", "-lcudart", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return out

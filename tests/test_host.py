@@ -121,3 +121,90 @@ def test_partition_scenes():
         assert sorted(i for p in parts for i in p) == list(range(256))
         assert imbalance(counts, parts) < 1.02
     assert partition_scenes([5, 1, 1], 2) == [[0], [1, 2]]
+
+
+def _lib_block(lib, dims, origin, spacing, radius, mass, jitter, seed):
+    n = dims[0] * dims[1] * dims[2]
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    o = (C.c_double * 3)(*origin)
+    assert lib.mps_gen_block(dims[0], dims[1], dims[2], o, spacing, radius, mass, jitter, seed,
+                             pos.ctypes.data_as(C.c_void_p), vel.ctypes.data_as(C.c_void_p)) == 0
+    return pos, vel
+
+
+def _lib_walls(lib, lo, hi, spacing, radius, open_mask):
+    clo, chi = (C.c_double * 3)(*lo), (C.c_double * 3)(*hi)
+    n = lib.mps_gen_box_walls(clo, chi, spacing, radius, open_mask, None)
+    out = np.zeros((n, 4), np.float32)
+    lib.mps_gen_box_walls(clo, chi, spacing, radius, open_mask, out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def _lib_sphere(lib, center, R, spacing, radius):
+    c = (C.c_double * 3)(*center)
+    n = lib.mps_gen_sphere(c, R, spacing, radius, None)
+    out = np.zeros((n, 4), np.float32)
+    lib.mps_gen_sphere(c, R, spacing, radius, out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def test_numpy_generators_equal_the_library(mps):
+    """The NumPy scene generators (which build every scene without loading a CUDA library) give the
+    same bits as the library's C-ABI generators, on the benchmark configurations' arguments."""
+    from mps_cuda_gb300 import scenes
+    lib = mps._lib.load()
+    for args in (((32, 32, 32), (0.0, 0.0, 0.0), 0.02, 0.01, 1.0e-3 * 8, 0.002, 0),
+                 ((100, 100, 100), (0.0, 0.0, 0.0), 0.01, 0.005, 1.0e-3, 0.001, 0),
+                 ((7, 3, 5), (1.25, -0.5, 0.1), 0.02, 0.01, 8.0, 0.002, 123456789012345),
+                 ((128, 125, 125), (0.49, 0.365, 0.365), 0.01, 0.005, 1.0e-3, 0.001, 1)):
+        pa, va = scenes.gen_block(*args)
+        pb, vb = _lib_block(lib, *args)
+        assert np.array_equal(pa.view(np.uint32), pb.view(np.uint32)), args[0]
+        assert np.array_equal(va.view(np.uint32), vb.view(np.uint32)), args[0]
+    for args in (((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), 0.02, 0.01, 0),
+                 ((0.0, 0.0, 0.0), (3.0, 1.5, 2.0), 0.01, 0.005, scenes.FACE_PY),
+                 ((0.0, 0.0, 0.0), (4.0, 2.0, 2.0), 0.01, 0.005, 0),
+                 ((-4.1, -3.9, -4.2), (3.3, 3.1, 3.05), 0.2, 0.1, 0b101001)):
+        a = scenes.gen_walls(*args)
+        b = _lib_walls(lib, *args)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), args
+    for args in (((2.0, 1.0, 1.0), 0.2, 0.01, 0.005), ((0.0, 0.0, 0.0), 1.0, 0.05, 0.01)):
+        a = scenes.gen_sphere(*args)
+        b = _lib_sphere(lib, *args)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), args
+
+
+def test_scene_construction_loads_no_cuda_library():
+    """Building the benchmark scenes maps no CUDA library, so the reference arm of bench.py can
+    build its inputs and map only the reference's own step (checked in a fresh interpreter)."""
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from mps_cuda_gb300 import scenes\n"
+            "scenes.dam_break_32k(); scenes.colliding_4m(scale=0.05); scenes.reference_surface_tension()\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libmps_gb300' not in maps and 'libcudart' not in maps, 'a CUDA library was mapped'\n"
+            "print('ok')\n") % str(ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr
+
+
+def test_noalloc_sort_rejects_bad_arguments_before_device_work(mps):
+    """The allocation-free cell sort checks its sizes and its pointers' alignment on the host and
+    touches no device before rejecting them (pointer values here are never dereferenced)."""
+    lib = mps._lib.load()
+    origin = (C.c_float * 3)(0.0, 0.0, 0.0)
+    dims = (C.c_int32 * 3)(4, 4, 4)
+    ok = dict(pos=0x10000, keys=0x20000, order=0x30000)
+
+    def call(n, pos=ok["pos"], keys=ok["keys"], order=ok["order"], cell=1.0):
+        return lib.mps_cell_sort_noalloc(C.c_void_p(pos), n, origin, C.c_float(cell), dims, C.c_void_p(keys),
+                                         C.c_void_p(order), None)
+
+    assert call(262145) == -1                 # beyond the fixed scratch
+    assert call(-1) == -1
+    assert call(16, pos=0x10008) == -1        # float4 reads need 16-byte alignment
+    assert call(16, keys=0x20004) == -1       # 64-bit keys
+    assert call(16, order=0x30002) == -1      # 32-bit indices
+    assert call(16, cell=0.0) == -1
