@@ -80,7 +80,7 @@ void mps_handle::release() {
                      (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&rho, (void**)&rdev,
                      (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
-                     (void**)&bpos, (void**)&bvol,
+                     (void**)&bpos, (void**)&bvol, (void**)&bvol_lo,
                      (void**)&partial, (void**)&acc, (void**)&nbr_t, (void**)&tile_j, (void**)&tile_n, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
                      (void**)&keys, (void**)&keys_tmp, (void**)&vals, (void**)&vals_tmp, (void**)&sort_counts,
                      (void**)&stage_pos, (void**)&stage_vel};
@@ -117,6 +117,7 @@ Params make_params(const mps_handle* h) {
     p.rho0 = float(m.density);
     p.inv_rho0 = float(1.0 / m.density);
     p.V = float(m.volume);
+    p.V_lo = float(m.volume - double(p.V));
     p.visc = float(m.viscosity);
     p.xsph = float(m.xsph);
     p.sigma = float(m.surface_tension);
@@ -180,6 +181,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.tape_adv = nullptr;
     d.bpos = h->bpos;
     d.bvol = h->bvol;
+    d.bvol_lo = h->bvol_lo;
     d.partial = h->partial;
     d.acc = h->acc;
     d.nbr_t = h->nbr_t;
@@ -301,6 +303,7 @@ int allocate(mps_handle* h) {
     }
     MPS_CUDA_TRY(dalloc(&h->bpos, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->bvol, size_t(std::max<int64_t>(h->nb, 1))));
+    MPS_CUDA_TRY(dalloc(&h->bvol_lo, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->partial, 2 * (S / 64 + 1)));
     // the loop-sum accumulators start at zero; each decide kernel zeroes what it has read (one
     // region more than the scenes: the profiling forms of the pass kernels add into it, unread)
@@ -353,10 +356,13 @@ int upload_boundary(mps_handle* h) {
     std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
     h->bperm = ord;
     std::vector<float4> bp(static_cast<size_t>(nb));
-    std::vector<float> bv(size_t(nb), 0.0f);
+    std::vector<float> bv(size_t(nb), 0.0f), bvl(size_t(nb), 0.0f);
     for (int64_t k = 0; k < nb; ++k) {
         bp[size_t(k)] = h->bpos_user[ord[size_t(k)]];
-        if (h->bvol_given) bv[size_t(k)] = h->bvol_user[ord[size_t(k)]];
+        if (h->bvol_given) {
+            bv[size_t(k)] = h->bvol_user[ord[size_t(k)]];
+            bvl[size_t(k)] = h->bvol_user_lo[ord[size_t(k)]];
+        }
     }
     std::vector<uint2> table(size_t(h->total_cells), make_uint2(0u, 0u));
     for (int64_t k = 0; k < nb; ++k) {
@@ -368,6 +374,7 @@ int upload_boundary(mps_handle* h) {
     if (nb > 0) {
         MPS_CUDA_TRY(cudaMemcpy(h->bpos, bp.data(), size_t(nb) * sizeof(float4), cudaMemcpyHostToDevice));
         MPS_CUDA_TRY(cudaMemcpy(h->bvol, bv.data(), size_t(nb) * sizeof(float), cudaMemcpyHostToDevice));
+        MPS_CUDA_TRY(cudaMemcpy(h->bvol_lo, bvl.data(), size_t(nb) * sizeof(float), cudaMemcpyHostToDevice));
     }
     MPS_CUDA_TRY(cudaMemcpy(h->btable, table.data(), table.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     if (!h->bvol_given && nb > 0) {
@@ -898,8 +905,12 @@ int mps_set_boundary(mps_handle* h, int64_t nb, const double* pos3, const double
         h->bpos_user[size_t(i)] = make_float4(float(pos3[3 * i]), float(pos3[3 * i + 1]), float(pos3[3 * i + 2]), float(radius[i]) * kHRatio);
     h->bvol_given = volume != nullptr;
     h->bvol_user.assign(size_t(nb), 0.0f);
+    h->bvol_user_lo.assign(size_t(nb), 0.0f);
     if (volume)
-        for (int64_t i = 0; i < nb; ++i) h->bvol_user[size_t(i)] = float(volume[i]);
+        for (int64_t i = 0; i < nb; ++i) {
+            h->bvol_user[size_t(i)] = float(volume[i]);
+            h->bvol_user_lo[size_t(i)] = float(volume[i] - double(h->bvol_user[size_t(i)]));   // the pair's low part
+        }
     h->have_boundary = true;
     if (h->layout_ready) {
         // re-layout with the new boundary while keeping the fluid
@@ -1087,6 +1098,8 @@ int mps_put_field(mps_handle* h, const char* name, const void* src, int order) {
             std::memcpy(tmp.data() + size_t(k) * pe, in + from * pe, pe);
         }
         if (h->nb) MPS_CUDA_TRY(cudaMemcpy(f.base, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
+        // a volume put as FP32 is exact: its float-float low part is zero
+        if (h->nb && f.base == h->bvol) MPS_CUDA_TRY(cudaMemset(h->bvol_lo, 0, size_t(h->nb) * sizeof(float)));
         return MPS_OK;
     }
     std::vector<unsigned char> tmp(size_t(h->slots) * pe);

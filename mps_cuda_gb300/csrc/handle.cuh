@@ -57,6 +57,7 @@ struct mps_handle {
     float2* cg_coef = nullptr;
     float4* bpos = nullptr;
     float* bvol = nullptr;
+    float* bvol_lo = nullptr;           // low part of the boundary volume as a float-float pair
     double* partial = nullptr;
     unsigned long long* acc = nullptr;
     unsigned short* nbr_t = nullptr;
@@ -75,7 +76,7 @@ struct mps_handle {
 
     std::vector<uint32_t> bperm;        // sorted boundary index -> user boundary index
     std::vector<float4> bpos_user;      // boundary positions as given (x,y,z,h) in user order
-    std::vector<float> bvol_user;
+    std::vector<float> bvol_user, bvol_user_lo;
 
     cudaStream_t cap_stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (cur, nsteps) -> exec

@@ -87,6 +87,7 @@ struct Params {
     float dt, inv_dt;
     float gx, gy, gz;
     float rho0, inv_rho0, V;      // rest density, particle volume
+    float V_lo;                   // volume - V (the float-float density deviation)
     float visc, xsph, sigma;
     float cg_factor;
     int cubic;
@@ -143,6 +144,7 @@ struct Dev {
     unsigned char* tape_adv;      // adjoint recording: collision branch per slot (2 bits per axis)
     const float4* bpos;           // boundary (x, y, z, h)
     float* bvol;
+    float* bvol_lo;               // bvol + bvol_lo = the volume to about 48 bits (the density deviation)
     double* partial;              // per-block partial sums of the CG operator pass and the Jacobi sweep
     unsigned long long* acc;      // loop-sum accumulators: (scenes + 1) x kAccLanes x kAccStride words
     unsigned short* nbr_t;        // stage 1: tile rank of each fluid neighbour, interleaved like nbr_f
@@ -230,6 +232,89 @@ struct Kahan {
         s = t;
     }
 };
+
+// Float-float ("double-float") arithmetic: a value is hi + lo with |lo| <= ulp(hi) / 2, about 48
+// significant bits, from error-free transformations in FP32 (explicit round-to-nearest intrinsics,
+// so that no contraction changes them).  Used where FP32 loses the result in a cancellation and
+// FP64, a small fraction of FP32's rate on GB300, would be the slow part: the density deviation
+// rho/rho0 - 1 that the stiffness reads.
+struct ff {
+    float hi, lo;
+};
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {   // a + b exactly
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const ff s = ff_two_sum(a.hi, b.hi);
+    return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return ff_fast_two_sum(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ ff ff_mul(ff a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    return ff_fast_two_sum(p, __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p)));
+}
+__device__ __forceinline__ ff ff_sqr_diff(float a, float b) {   // (a - b)^2 with a - b exact as a pair
+    const ff d = ff_two_sum(a, -b);
+    return ff_mul(d, d);
+}
+__device__ __forceinline__ float ff_val(ff a) { return __fadd_rn(a.hi, a.lo); }
+// 1/h as a pair: hi the rounded reciprocal, lo its residual (1 - h hi) / h.
+__device__ __forceinline__ ff ff_recip(float h) {
+    const float r = 1.0f / h;
+    return {r, __fmul_rn(__fmaf_rn(-h, r, 1.0f), r)};
+}
+// Constants of the kernels as pairs (hi = the FP32 rounding of c, lo = c - hi), from FP64.
+#define MPSG_FF_CONST(c) ff{float(c), float((c) - double(float(c)))}
+constexpr double kPiD = 3.14159265358979323846;
+// Per-particle scales of ff_VW: V c invh^3 for the kernel's branches (cubic: c = 16/pi for q >= 1/2,
+// 8/pi below; poly6: c = 315 / (64 pi)), so that a pair needs one product for them.
+struct FFScale {
+    ff outer, inner;
+};
+__device__ __forceinline__ FFScale ff_scales(ff invh, ff V, int cubic) {
+    const ff v3 = ff_mul(ff_mul(ff_mul(invh, invh), invh), V);
+    if (cubic) return {ff_mul(v3, MPSG_FF_CONST(16.0 / kPiD)), ff_mul(v3, MPSG_FF_CONST(8.0 / kPiD))};
+    const ff w = ff_mul(v3, MPSG_FF_CONST(315.0 / (64.0 * kPiD)));
+    return {w, w};
+}
+// V W(|x_i - x_j|) in float-float, with invh = 1/h_i and the scales of ff_scales: the squared
+// distance exactly from the FP32 positions, its square root to about 48 bits, then the kernel
+// polynomial (MPSSPHKernel.cuh:28-45) in pairs.
+__device__ __forceinline__ ff ff_VW(float4 xi, float4 xj, ff invh, const FFScale& sc, int cubic) {
+    const ff d2 = ff_add(ff_add(ff_sqr_diff(xi.x, xj.x), ff_sqr_diff(xi.y, xj.y)), ff_sqr_diff(xi.z, xj.z));
+    if (cubic) {
+        // d = sqrt(d2): hi the rounded root, lo = (d2 - hi^2) / (2 hi)
+        ff d{0.0f, 0.0f};
+        if (d2.hi > 0.0f) {
+            const float r = sqrtf(d2.hi);
+            d = ff_fast_two_sum(r, __fmul_rn(__fadd_rn(__fmaf_rn(-r, r, d2.hi), d2.lo), __fdividef(0.5f, r)));
+        }
+        const ff q = ff_mul(d, invh);
+        if (q.hi >= 1.0f) return ff{0.0f, 0.0f};
+        if (q.hi >= 0.5f) {   // V 2 cw invh^3 (1 - q)^3; 1 - q.hi is exact for q in [0.5, 1]
+            const ff t = ff_fast_two_sum(__fsub_rn(1.0f, q.hi), -q.lo);
+            return ff_mul(ff_mul(ff_mul(t, t), t), sc.outer);
+        }
+        // V cw invh^3 ((6 q - 6) q^2 + 1)
+        const ff q6 = ff_add(ff_mul(q, 6.0f), ff{-6.0f, 0.0f});
+        return ff_mul(ff_add(ff_mul(ff_mul(q6, q), q), ff{1.0f, 0.0f}), sc.inner);
+    }
+    // poly6: V w invh^3 (1 - q^2)^3 with q^2 = d2 invh^2
+    const ff q2 = ff_mul(ff_mul(d2, invh), invh);
+    if (q2.hi >= 1.0f) return ff{0.0f, 0.0f};
+    const ff t = ff_add(ff{1.0f, 0.0f}, ff{-q2.hi, -q2.lo});
+    return ff_mul(ff_mul(ff_mul(t, t), t), sc.outer);
+}
 
 // Neighbour loops are latency-bound (a dependent index load, then gathers).  visit_batched walks
 // the interleaved list of slot i (item k at list[k * stride + i]) in batches of B: phase 1 loads

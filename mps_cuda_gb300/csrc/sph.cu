@@ -29,6 +29,7 @@ constexpr unsigned kFull = 0xffffffffu;
 struct XV { float4 x, v; };
 struct XVA { float4 x, v; float2 a; };
 struct XQ { float4 x, q; };
+struct XB { float4 x; float lo; };   // boundary position + volume, and the volume's low part
 
 // Programmatic dependent launch between a decide kernel and the vector pass after it: the decide
 // kernel releases its dependent as it starts; the vector pass loads its vectors (written by kernels
@@ -369,6 +370,11 @@ __device__ __forceinline__ void pair_dist(float d2, float& dist, float& invd) {
         dist = d2 * invd;
     }
 }
+// Density sums of the density pass as float-float pairs (ff_VW): the deviation rho/rho0 - 1, which
+// the stiffness reads, to about 1e-8 instead of the 2e-7 of FP32 kernel values and distances.
+#ifndef MPSG_DENSITY_FF
+#define MPSG_DENSITY_FF 1
+#endif
 // Compensated (Kahan) sums of the density change rate in pressure pass A: delta is a sum of terms
 // of both signs whose result is small against them, and the stiffness is delta against rho/rho0 - 1.
 #ifndef MPSG_DELTA_KAHAN
@@ -526,7 +532,9 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
 }
 
 // ------------------------------------------------------------------ boundary volume
-// V_b = 1 / (prev + W(0) + sum_k W(|x_b - x_k|)) over boundary neighbours (Akinci).
+// V_b = 1 / (prev + W(0) + sum_k W(|x_b - x_k|)) over boundary neighbours (Akinci,
+// MPSSPHBaseUtil.cuh:10-86), with the sums and the reciprocal in float-float pairs: the volume is
+// stored as bvol + bvol_lo, which the density deviation reads.
 __global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb) return;
@@ -537,12 +545,12 @@ __global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
     }
     const Scene& sc = d.scenes[lo];
     const float4 xi = d.bpos[b];
-    const float invh = 1.0f / xi.w;
+    const ff invh = ff_recip(xi.w);
+    const FFScale scl = ff_scales(invh, ff{1.0f, 0.0f}, p.cubic);
     const int cx = cell_coord(xi.x, sc.ox, sc.inv_cell, sc.nx);
     const int cy = cell_coord(xi.y, sc.oy, sc.inv_cell, sc.ny);
     const int cz = cell_coord(xi.z, sc.oz, sc.inv_cell, sc.nz);
-    Kahan sum;
-    sum.add(kW(0.0f, invh, p.cubic));
+    ff sum = ff_VW(xi, xi, invh, scl, p.cubic);
     for (int z = max(cz - 1, 0); z <= min(cz + 1, sc.nz - 1); ++z)
         for (int y = max(cy - 1, 0); y <= min(cy + 1, sc.ny - 1); ++y)
             for (int x = max(cx - 1, 0); x <= min(cx + 1, sc.nx - 1); ++x) {
@@ -553,11 +561,16 @@ __global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
                     const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
                     const float d2 = dist2(dx, dy, dz);
                     const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
-                    if (d2 < __fmul_rn(hij, hij)) sum.add(kW(sqrtf(d2), invh, p.cubic));
+                    if (d2 < __fmul_rn(hij, hij)) sum = ff_add(sum, ff_VW(xi, xj, invh, scl, p.cubic));
                 }
             }
-    const float prev = accumulate ? d.bvol[b] : 0.0f;
-    d.bvol[b] = 1.0f / (prev + sum.s);
+    if (accumulate) sum = ff_add(sum, ff{d.bvol[b], d.bvol_lo[b]});
+    // 1 / sum as a pair: r = 1 / hi, then the residual (1 - sum r) r
+    const float r = 1.0f / sum.hi;
+    const float e = __fsub_rn(__fmaf_rn(-sum.hi, r, 1.0f), __fmul_rn(sum.lo, r));
+    const ff v = ff_fast_two_sum(r, __fmul_rn(e, r));
+    d.bvol[b] = v.hi;
+    d.bvol_lo[b] = v.lo;
 }
 
 // ------------------------------------------------------------------ density + alpha + gravity
@@ -580,14 +593,27 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p, int parts
         const unsigned c = d.cnt[i];
         const int nf = (parts & 1) ? int(c & 0xffffu) : 0, nb = (parts & 2) ? int(c >> 16) : 0;
         Kahan rf, gx, gy, gz, sq;
+#if MPSG_DENSITY_FF
+        // the density sums as float-float pairs (the deviation rho/rho0 - 1 is a small difference)
+        const ff invh2 = ff_recip(xi.w);
+        const FFScale scf = ff_scales(invh2, ff{p.V, p.V_lo}, p.cubic);   // fluid terms
+        const FFScale scb = ff_scales(invh2, ff{1.0f, 0.0f}, p.cubic);    // boundary terms (times V_b)
+        ff sf{0.0f, 0.0f}, sb{0.0f, 0.0f};
+        if ((WHAT & W_DENSITY) && (parts & 1)) sf = ff_VW(xi, xi, invh2, scf, p.cubic);
+#else
         if (parts & 1) rf.add(p.V * kW(0.0f, invh, p.cubic));
+#endif
         visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_f, stride, i, nf, [&](int) { return NoStream{}; }, [&](unsigned j, int) { return d.pos[j]; },
                               [&](const float4& xj, NoStream, int) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             float dist, invd;
             pair_dist<MPSG_EXACT_DIST_DENS>(d2, dist, invd);
+#if MPSG_DENSITY_FF
+            if (WHAT & W_DENSITY) sf = ff_add(sf, ff_VW(xi, xj, invh2, scf, p.cubic));
+#else
             if (WHAT & W_DENSITY) rf.add(p.V * kW(dist, invh, p.cubic));
+#endif
             if (WHAT & W_ALPHA) {
                 const float g = p.V * kG(dist, invd, invh, p.cubic);
                 const float ax = g * dx, ay = g * dy, az = g * dz;
@@ -596,26 +622,42 @@ __global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p, int parts
             }
         });
         Kahan rb;
-        visit_batched<MPSG_B_DENS, NoStream, float4, MPSG_PF_DENS>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
-                              [&](unsigned j, int) { float4 x = d.bpos[j]; x.w = d.bvol[j]; return x; },
-                              [&](const float4& xj, NoStream, int) {
+        visit_batched<MPSG_B_DENS, NoStream, XB, MPSG_PF_DENS>(d.nbr_b, stride, i, nb, [&](int) { return NoStream{}; },
+                              [&](unsigned j, int) {
+                                  float4 x = d.bpos[j];
+                                  x.w = d.bvol[j];
+                                  return XB{x, (WHAT & W_DENSITY) ? d.bvol_lo[j] : 0.0f};
+                              },
+                              [&](const XB& xb, NoStream, int) {
+            const float4 xj = xb.x;
             const float vb = xj.w;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             float dist, invd;
             pair_dist<MPSG_EXACT_DIST_DENS>(d2, dist, invd);
+#if MPSG_DENSITY_FF
+            if (WHAT & W_DENSITY) sb = ff_add(sb, ff_mul(ff_VW(xi, xj, invh2, scb, p.cubic), ff{vb, xb.lo}));
+#else
             if (WHAT & W_DENSITY) rb.add(vb * kW(dist, invh, p.cubic));
+#endif
             if (WHAT & W_ALPHA) {
                 const float g = vb * kG(dist, invd, invh, p.cubic);
                 gx.add(g * dx); gy.add(g * dy); gz.add(g * dz);
             }
         });
         if (WHAT & W_DENSITY) {
+#if MPSG_DENSITY_FF
+            const ff tot = ff_add(sf, sb);
+            rho = ff_val(tot) * p.rho0;
+            d.rho[i] = rho;
+            d.rdev[i] = ff_val(ff_add(tot, ff{-1.0f, 0.0f}));
+#else
             rho = (rf.s + rb.s) * p.rho0;
             d.rho[i] = rho;
             // rho / rho0 - 1 without the rounding of rho itself: rf.s - 1 is exact (Sterbenz), and
             // the Kahan sums carry their lost low parts in c (true sum = s - c)
             d.rdev[i] = __fsub_rn(__fadd_rn(__fsub_rn(rf.s, 1.0f), rb.s), __fadd_rn(rf.c, rb.c));
+#endif
         }
         if (WHAT & W_ALPHA) {
             // alpha denominator in FP64: |sum grad|^2 + sum |grad|^2, clamp at 1e-20
@@ -1691,7 +1733,21 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long 
     (void)bs;
     launch_after_decide(k_cg_update<256>, p.slots / 256, 256, s, d, p, cond, use_cond, limit);
 }
+// Preferred shared-memory carveout (percent) of the plain CG operator, which uses almost no shared
+// memory: -1 leaves the driver's choice.
+#ifndef MPSG_CG_CARVEOUT
+#define MPSG_CG_CARVEOUT -1
+#endif
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s) {
+#if MPSG_CG_CARVEOUT >= 0
+    static bool carveout_set = false;
+    if (!carveout_set) {
+        cudaFuncSetAttribute(k_cg_ap3<64>, cudaFuncAttributePreferredSharedMemoryCarveout, MPSG_CG_CARVEOUT);
+        cudaFuncSetAttribute(k_cg_ap3<128>, cudaFuncAttributePreferredSharedMemoryCarveout, MPSG_CG_CARVEOUT);
+        cudaFuncSetAttribute(k_cg_ap3<256>, cudaFuncAttributePreferredSharedMemoryCarveout, MPSG_CG_CARVEOUT);
+        carveout_set = true;
+    }
+#endif
     if (p.stage == 1) {
         const size_t sm = size_t(2 * kTilePerSlot) * size_t(bs) * sizeof(float4);   // 40 KB at most (256 slots)
         if (bs == 128) k_cg_ap3_tile<128><<<p.slots / 128, 128, sm, s>>>(d, p, cond, use_cond);

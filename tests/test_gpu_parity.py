@@ -6,6 +6,11 @@ Tolerances (FP32 bulk vs FP64 oracle, same inputs):
     reference's FP64 test differ only for pairs within 1e-6 h of the support radius.
   - densities, alphas, pressure factors, velocities after a phase, from an identical state:
     max|a - b| / max|b| <= 1e-5 (the north-star bound "1e-5 relative of an FP64 oracle").
+    "Identical state": the GPU's FP32 state is what both sides start from (the oracle takes it
+    exactly, FP32 values being FP64 values), before the step and before each solver phase.  The
+    pressure factor from an identical state is the stiffness of a solve's first iteration
+    (fixed_iters = 1); after further iterations the two sides' velocities already differ by their
+    own rounding.
 Solver phases are compared in fixed-iteration mode (same number of Jacobi / CG iterations on
 both sides) and, in adaptive mode, by iteration counts within one iteration.
 """
@@ -30,6 +35,17 @@ def make(mps, orc, scene, **cfg):
     sim = Simulation.from_scene(scene, **cfg)
     o = orc.from_scene(scene, config=cfg)
     return sim, o
+
+
+def gpu_state_to_oracle(sim, o):
+    """The oracle continues from the GPU's current (FP32) fluid state."""
+    p, v = sim.get_fluid()
+    o.set_fluid(p[:, :3].astype(np.float64), v[:, :3].astype(np.float64), v[:, 3].astype(np.float64),
+                p[:, 3].astype(np.float64))
+
+
+def gpu_vel_to_oracle(sim, o):
+    o.put("vel", sim.get_field("vel")[:, :3].astype(np.float64))
 
 
 def advance_to_density(sim, o, mps):
@@ -110,16 +126,14 @@ def test_density_alpha_gravity(mps, orc, small):
     assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL
 
 
-@pytest.mark.parametrize("fixed", [0, 4])
+@pytest.mark.parametrize("fixed", [0, 1, 4])
 def test_pressure_and_nonpressure_solves(mps, orc, small, fixed):
     sim, o = make(mps, orc, small, fixed_iters=fixed)
     advance_to_density(sim, o, mps)
-    # from an identical state: the oracle's velocities go into the GPU before each solve
+    # each solve from an identical state: the GPU's velocities go into the oracle before it
     for gph, oph, name in ((mps.PHASE_DF, orc.DF, "df_iters"), (mps.PHASE_VISCST, orc.VISCST, "cg_iters"),
                            (mps.PHASE_CD, orc.CD, "cd_iters")):
-        v = sim.get_field("vel")
-        v[:, :3] = o.get("vel")
-        sim.put_field("vel", v)
+        gpu_vel_to_oracle(sim, o)
         sim.phase(gph)
         o.phase(oph)
         gi, oi = sim.stats()[name], o.stats()[name]
@@ -129,8 +143,9 @@ def test_pressure_and_nonpressure_solves(mps, orc, small, fixed):
             assert abs(gi - oi) <= 1, (name, gi, oi)
         if gi == oi:
             assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL, name
-    if fixed:
-        assert rel_err(sim.get_field("pressure"), o.get("pressure")) < 1e-4
+        if fixed == 1 and name != "cg_iters":
+            # the stiffness of the solve's one iteration, from an identical state
+            assert rel_err(sim.get_field("pressure"), o.get("pressure")) < REL, name
 
 
 def test_advect(mps, orc, small):
@@ -139,9 +154,7 @@ def test_advect(mps, orc, small):
     for gph, oph in ((mps.PHASE_DF, orc.DF), (mps.PHASE_VISCST, orc.VISCST), (mps.PHASE_CD, orc.CD)):
         sim.phase(gph)
         o.phase(oph)
-    v = sim.get_field("vel")
-    v[:, :3] = o.get("vel")
-    sim.put_field("vel", v)
+    gpu_vel_to_oracle(sim, o)
     sim.phase(mps.PHASE_ADVECT)
     o.phase(orc.ADVECT)
     assert rel_err(sim.get_field("pos")[:, :3], o.get("pos")) < 1e-6
@@ -196,24 +209,34 @@ def test_full_step_vs_oracle_fixed_iterations(mps, orc, small):
     o.step(1)
     p, v = sim.get_fluid()
     assert rel_err(p[:, :3], o.get("pos")) < 1e-6
-    assert rel_err(v[:, :3], o.get("vel")) < 1e-4
+    assert rel_err(v[:, :3], o.get("vel")) < REL
     assert rel_err(sim.get_field("density"), o.get("density")) < REL
 
 
 def test_reference_scene_step(mps, orc):
-    """The reference's own scene (poly6/spiky, reference material, shipped tolerances)."""
+    """The reference's own scene (poly6/spiky, reference material, shipped tolerances), frame by
+    frame from an identical state: the same iteration counts (or within one where a residual
+    lands on the tolerance) and, where they are equal, the same positions and velocities."""
     from mps_cuda_gb300 import Simulation, scenes
     sc = scenes.reference_surface_tension()
     sim = Simulation.from_scene(sc)
     o = orc.from_scene(sc)
-    for f in range(3):
+    equal = 0
+    for f in range(6):
+        gpu_state_to_oracle(sim, o)
+        o.set_frame(f)
         sim.step(1)
         o.step(1)
         st, ost = sim.stats(), o.stats()
-        assert abs(st["df_iters"] - ost["df_iters"]) <= 1
-        assert abs(st["cd_iters"] - ost["cd_iters"]) <= 2
-    p, v = sim.get_fluid()
-    assert rel_err(p[:, :3], o.get("pos")) < 1e-4
+        its = (st["df_iters"], st["cg_iters"], st["cd_iters"])
+        oits = (ost["df_iters"], ost["cg_iters"], ost["cd_iters"])
+        assert all(abs(a - b) <= 1 for a, b in zip(its, oits)), (f, its, oits)
+        if its == oits:
+            equal += 1
+            p, v = sim.get_fluid()
+            assert rel_err(p[:, :3], o.get("pos")) < 1e-6, f
+            assert rel_err(v[:, :3], o.get("vel")) < REL, f
+    assert equal >= 4
 
 
 @pytest.mark.parametrize("form", [0, 1])
@@ -238,17 +261,29 @@ def test_batched_equals_single(mps, form):
 
 
 def test_step_host_matches_device_step(mps):
+    """The host-buffer call (load the state, step, store it) equals the same load + step through the
+    device API bit for bit; against a run that keeps its cell order between steps it differs only by
+    rounding (a reload starts from particle-ID order, which changes the order within each cell and
+    so the summation order)."""
     from mps_cuda_gb300 import Simulation, scenes
     sc = scenes.dam_break_small(8, seed=6)
     a = Simulation.from_scene(sc)
     b = Simulation.from_scene(sc)
+    c = Simulation.from_scene(sc)
     a.step(2)
     p = sc.pos4.copy()
     v = sc.vel4.copy()
     b.step_host(p, v, 1)
+    p1, v1 = p.copy(), v.copy()
     b.step_host(p, v, 1)
+    c.step(1)
+    c.set_fluid(p1, v1)
+    c.step(1)
+    pc, vc = c.get_fluid()
+    assert np.array_equal(p, pc) and np.array_equal(v, vc)
     pa, va = a.get_fluid()
-    assert np.allclose(p, pa, atol=0, rtol=0) or rel_err(p[:, :3], pa[:, :3]) < 1e-6
+    assert rel_err(p[:, :3], pa[:, :3]) < 1e-6
+    assert rel_err(v[:, :3], va[:, :3]) < REL
 
 
 @pytest.mark.parametrize("form", [0, 1])
@@ -308,7 +343,7 @@ def test_single_particle_and_single_pair(mps, orc):
         o.step(2)
         p, v = sim.get_fluid()
         assert rel_err(p[:, :3], o.get("pos")) < 1e-6, keep
-        assert rel_err(v[:, :3], o.get("vel")) < 1e-4, keep
+        assert rel_err(v[:, :3], o.get("vel")) < REL, keep
 
 
 def test_batched_with_an_empty_scene(mps):
@@ -352,9 +387,7 @@ def test_cg_forms_match_oracle(mps, orc, fixed):
         advance_to_density(sim, o, mps)
         sim.phase(mps.PHASE_DF)
         o.phase(orc.DF)
-        v = sim.get_field("vel")
-        v[:, :3] = o.get("vel")
-        sim.put_field("vel", v)
+        gpu_vel_to_oracle(sim, o)
         sim.phase(mps.PHASE_VISCST)
         o.phase(orc.VISCST)
         gi, oi = sim.stats()["cg_iters"], o.stats()["cg_iters"]
@@ -375,5 +408,38 @@ def test_reference_viscosity_scene_step(mps, orc):
         sim.step(1)
         o.step(1)
     p, v = sim.get_fluid()
-    assert rel_err(p[:, :3], o.get("pos")) < 1e-5
-    assert rel_err(v[:, :3], o.get("vel")) < 1e-4
+    assert rel_err(p[:, :3], o.get("pos")) < 1e-6
+    assert rel_err(v[:, :3], o.get("vel")) < REL
+
+
+@pytest.mark.parametrize("warm", [0, 30])
+def test_dam_break_32k_phase_by_phase(mps, orc, warm):
+    """The 32k dam break configuration at full size (32^3 fluid, the 51^3 wall lattice, cubic
+    spline, 0.1 % tolerances), phase by phase against the oracle from an identical state: at the
+    first step and after `warm` GPU steps.  Density and alpha after the density pass; the pressure
+    factor of each pressure solve's first iteration (fixed_iters = 1) and the velocities after
+    each solve (adaptive, where the iteration counts agree)."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_32k(seed=0)
+    for fixed in (1, 0):
+        sim = Simulation.from_scene(sc, fixed_iters=fixed)
+        if warm:
+            sim.step(warm)
+        o = orc.from_scene(sc, config=dict(fixed_iters=fixed))
+        gpu_state_to_oracle(sim, o)
+        advance_to_density(sim, o, mps)
+        rho0 = sc.material["density"]
+        assert np.abs(sim.get_field("density") - o.get("density")).max() / rho0 < REL
+        assert rel_err(sim.get_field("alpha"), o.get("alpha")) < REL
+        for gph, oph, name in ((mps.PHASE_DF, orc.DF, "df_iters"), (mps.PHASE_VISCST, orc.VISCST, "cg_iters"),
+                               (mps.PHASE_CD, orc.CD, "cd_iters")):
+            gpu_vel_to_oracle(sim, o)
+            sim.phase(gph)
+            o.phase(oph)
+            gi, oi = sim.stats()[name], o.stats()[name]
+            assert abs(gi - oi) <= (0 if fixed else 1), (name, gi, oi)
+            if gi == oi:
+                assert rel_err(sim.get_field("vel")[:, :3], o.get("vel")) < REL, (name, fixed)
+            if fixed and name != "cg_iters":
+                assert rel_err(sim.get_field("pressure"), o.get("pressure")) < REL, name
+        sim.close()
