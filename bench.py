@@ -159,7 +159,7 @@ def cpu_baseline(scene, pos4, vel4, gpu_iters, budget_s: float = 12.0, max_steps
 def run_ours(args, scene, rank, world, local_rank):
     import torch
     from mps_cuda_gb300 import Simulation, build
-    from mps_cuda_gb300._lib import K_CG_AP, K_CG_VECTOR, K_PRESSURE_A, K_PRESSURE_B
+    from mps_cuda_gb300._lib import K_BUILD_NBRS, K_CG_AP, K_CG_VECTOR, K_DENSITY_ALPHA, K_PRESSURE_A, K_PRESSURE_B
 
     build.build()
     dist = world > 1
@@ -248,6 +248,9 @@ def run_ours(args, scene, rank, world, local_rank):
     if not args.cg_form:  # three-pass CG (default): its update + direction passes
         per["cg_vector"] = sim.profile_kernel(K_CG_VECTOR, reps, stream)
         shares["cg_vector"] = per["cg_vector"] * runs[1]
+    # once-a-step passes (not roofline candidates: no per-launch byte count is claimed for them)
+    once = {"build_nbrs": sim.profile_kernel(K_BUILD_NBRS, 5, stream),
+            "density_alpha": sim.profile_kernel(K_DENSITY_ALPHA, 5, stream)}
     dom = max(shares, key=shares.get)
     bnd = scene.nb if dom.startswith("pressure") else 0
     algo = ALGO_BYTES[dom] * scene.n + BOUNDARY_BYTES * bnd
@@ -275,7 +278,7 @@ def run_ours(args, scene, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": src, "traffic": traffic, "traffic_source": "profiles/dram_traffic.json (ncu capture at 512k particles scaled to 1M)" if traffic else None,
                      "algorithmic_bytes_per_launch": algo, "ms_per_launch": per[dom],
-                     "ms_per_launch_all": per,
+                     "ms_per_launch_all": per, "ms_per_launch_once_a_step": once,
                      "solver_loop_kernels_ms_per_step": sum(shares.values()) / args.steps},
         "step_roofline": {"algorithmic_bytes_per_step": step_algo,
                           "achieved_gbs": step_algo / (ms_max / args.steps / 1e3) / 1e9},
@@ -585,12 +588,38 @@ def run_adjoint(args, rank, world, local_rank):
     return line
 
 
-def _step_vs_oracle(sim, o, scene, mps, orc):
-    """One step from an identical state on both sides, phase by phase; per-quantity errors."""
+def _step_vs_oracle(sim, o, scene, mps, orc, sim1=None, o1=None):
+    """One step from an identical state on both sides, phase by phase; per-quantity errors.  Each
+    solver phase starts from the GPU's velocities on both sides.  With sim1 / o1 (fixed_iters = 1)
+    the stiffness of each pressure solve's first iteration is compared from the same state."""
     import numpy as np
     p, v = sim.get_fluid()
-    o.set_fluid(p[:, :3].astype(np.float64), v[:, :3].astype(np.float64), v[:, 3].astype(np.float64),
-                p[:, 3].astype(np.float64))
+
+    def to_oracle(oo):
+        oo.set_fluid(p[:, :3].astype(np.float64), v[:, :3].astype(np.float64), v[:, 3].astype(np.float64),
+                     p[:, 3].astype(np.float64))
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+    out = {}
+    if sim1 is not None:
+        sim1.set_fluid(p, v)
+        to_oracle(o1)
+        for ph in (mps.PHASE_SORT, mps.PHASE_NEIGHBORS, mps.PHASE_BVOLUME, mps.PHASE_DENSITY_ALPHA):
+            sim1.phase(ph)
+        for ph in (orc.ZSORT, orc.NEIGHBORS, orc.BVOLUME, orc.DENSITY, orc.ALPHA, orc.GRAVITY):
+            o1.phase(ph)
+        for gph, oph, name in ((mps.PHASE_DF, orc.DF, "df"), (mps.PHASE_VISCST, orc.VISCST, None),
+                               (mps.PHASE_CD, orc.CD, "cd")):
+            o1.put("vel", sim1.get_field("vel")[:, :3].astype(np.float64))
+            sim1.phase(gph)
+            o1.phase(oph)
+            if name:
+                out[f"pressure_{name}_first_iteration_max_rel"] = rel(sim1.get_field("pressure").astype(np.float64),
+                                                                      o1.get("pressure"))
+        sim1.phase(mps.PHASE_ADVECT)
+    to_oracle(o)
     for ph in (mps.PHASE_SORT, mps.PHASE_NEIGHBORS, mps.PHASE_BVOLUME, mps.PHASE_DENSITY_ALPHA):
         sim.phase(ph)
     for ph in (orc.ZSORT, orc.NEIGHBORS, orc.BVOLUME, orc.DENSITY, orc.ALPHA, orc.GRAVITY):
@@ -598,12 +627,15 @@ def _step_vs_oracle(sim, o, scene, mps, orc):
     rho0 = scene.material["density"]
     rg, ro = sim.get_field("density").astype(np.float64), o.get("density")
     ag, ao = sim.get_field("alpha").astype(np.float64), o.get("alpha")
-    out = {"density_max_rel": float(np.abs(rg - ro).max() / rho0),
-           "density_rms_rel": float(np.sqrt(np.mean((rg - ro) ** 2)) / rho0),
-           "alpha_max_rel": float(np.abs(ag - ao).max() / np.abs(ao).max())}
-    for gph, oph in ((mps.PHASE_DF, orc.DF), (mps.PHASE_VISCST, orc.VISCST), (mps.PHASE_CD, orc.CD)):
+    out.update({"density_max_rel": float(np.abs(rg - ro).max() / rho0),
+                "density_rms_rel": float(np.sqrt(np.mean((rg - ro) ** 2)) / rho0),
+                "alpha_max_rel": float(np.abs(ag - ao).max() / np.abs(ao).max())})
+    for gph, oph, name in ((mps.PHASE_DF, orc.DF, "df"), (mps.PHASE_VISCST, orc.VISCST, "cg"), (mps.PHASE_CD, orc.CD, "cd")):
+        o.put("vel", sim.get_field("vel")[:, :3].astype(np.float64))   # each solve from the same state
         sim.phase(gph)
         o.phase(oph)
+        vg, vo = sim.get_field("vel")[:, :3].astype(np.float64), o.get("vel")
+        out[f"velocity_after_{name}_max_rel"] = float(np.abs(vg - vo).max() / np.abs(vo).max())
     st, so = sim.stats(), o.stats()
     out["iters_gpu"] = [st["df_iters"], st["cg_iters"], st["cd_iters"]]
     out["iters_oracle"] = [so["df_iters"], so["cg_iters"], so["cd_iters"]]
@@ -632,8 +664,10 @@ def run_precision(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     sc = scenes.colliding_4m(seed=rank, scale=args.scale)
     sim = Simulation.from_scene(sc, device=local_rank, **overrides(args))
+    sim1 = Simulation.from_scene(sc, device=local_rank, fixed_iters=1, **overrides(args))
     threads = os.cpu_count() or 1
     o = orc.from_scene(sc, threads=threads)
+    o1 = orc.from_scene(sc, config=dict(fixed_iters=1), threads=threads)
     every = args.sample_every
     samples, gpu_ms, gpu_steps = [], 0.0, 0
     t_oracle = 0.0
@@ -642,7 +676,7 @@ def run_precision(args, rank, world, local_rank):
     while t < args.steps:
         if t % every == 0:
             t0 = time.perf_counter()
-            rec = _step_vs_oracle(sim, o, sc, mps, orc)
+            rec = _step_vs_oracle(sim, o, sc, mps, orc, sim1, o1)
             t_oracle += time.perf_counter() - t0
             rec["step"] = t
             samples.append(rec)
@@ -656,8 +690,9 @@ def run_precision(args, rank, world, local_rank):
         gpu_ms += e0.elapsed_time(e1)
         gpu_steps += k
         t += k
-    keys = ["density_max_rel", "density_rms_rel", "alpha_max_rel", "pressure_max_rel", "pressure_rms_rel",
-            "velocity_max_rel", "velocity_rms_rel"]
+    keys = ["density_max_rel", "density_rms_rel", "alpha_max_rel", "pressure_df_first_iteration_max_rel",
+            "pressure_cd_first_iteration_max_rel", "velocity_after_df_max_rel", "velocity_after_cg_max_rel",
+            "velocity_after_cd_max_rel", "pressure_max_rel", "pressure_rms_rel", "velocity_max_rel", "velocity_rms_rel"]
     same = [r for r in samples if r["iters_gpu"] == r["iters_oracle"]]
     line = {
         "metric": "particle-steps/s (DFSPH, 4M colliding blocks) + per-step error vs FP64",
@@ -666,7 +701,10 @@ def run_precision(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": sc.name, "fluid_particles": sc.n, "boundary_particles": sc.nb,
                    "sampled_every": every, "samples": len(samples), "oracle_threads": threads,
-                   "note": "timed steps are the graph steps between samples; sampled steps run phase by phase"},
+                   "note": "timed steps are the graph steps between samples; sampled steps run phase by phase, "
+                           "each solve from the GPU's velocities on both sides; *_first_iteration: the "
+                           "stiffness of a solve's first iteration from the same state (fixed_iters = 1); "
+                           "pressure_max_rel: the stiffness after the last iteration of the adaptive solve"},
         "max_over_samples": {k: max(r[k] for r in samples) for k in keys},
         "max_over_samples_equal_iterations": {k: max(r[k] for r in same) for k in keys} if same else None,
         "samples_with_equal_iterations": len(same),

@@ -42,6 +42,10 @@ if [ ! -d "$OUT/src/MPS_Computer" ]; then
     echo "reference sources unavailable (no $REF and no copy in $OUT/src)" >&2
     exit 2
 fi
+# without the reference tree, libraries built earlier from the copy are current
+if [ ! -d "$REF/src/MPS_Computer" ] && [ -f "$OUT/shipped/libmpsref.so" ] && [ -f "$OUT/config/libmpsref.so" ]; then
+    exit 0
+fi
 
 TUS="MPS_Computer/MPSSPHBaseUtil.cu MPS_Computer/MPSSPHDFSPHUtil.cu MPS_Computer/MPSSPHNonPressureUtil.cu MPS_Computer/MPSAdvectUtil.cu MPS_Object/MPSSpatialHash.cu"
 COMMON=(-std=c++20 --extended-lambda "-D__declspec(x)=" -Xcompiler -fPIC -gencode arch=compute_103a,code=sm_103a -O3

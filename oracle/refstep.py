@@ -18,7 +18,7 @@ def lib_path(variant: str) -> Path:
 
 
 def available(variant: str = "shipped") -> bool:
-    return lib_path(variant).exists() or (REF_DIR / "src" / "MPS_Computer").exists() or Path("/root/reference/src").exists()
+    return lib_path(variant).exists() or (REF_DIR / "src" / "MPS_Computer").exists()
 
 
 def build() -> None:
