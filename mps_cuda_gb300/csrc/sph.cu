@@ -531,176 +531,6 @@ __global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
     }
 }
 
-// Warp-staged neighbour search (the default).  A warp's 32 slots lie in a few neighbouring cells; the
-// warp stages the fluid and boundary particles of the box of cells around them (its cells grown by
-// one on every side) in shared memory once, then each lane scans its 27 cells from there in key
-// order, skipping cells whose box lies farther from the particle than the grid cell (the largest
-// pair cutoff).  Lists, their order and the counts are those of k_build_nbrs; a warp whose box or
-// particles exceed the staging space takes k_build_nbrs's global-memory path.
-constexpr int kWCells = 64;    // cells of a warp's box
-constexpr int kWFluid = 448;   // fluid particles staged per warp
-constexpr int kWBnd = 192;     // boundary particles staged per warp
-struct WCell {
-    unsigned fstart, bstart;   // first slot of the cell's fluid / boundary particles
-    unsigned short foff, fcnt; // staged position and count (fluid)
-    unsigned short boff, bcnt; // staged position and count (boundary)
-};
-// Squared distance from x to the box of cell (c + o) along one axis, with o in {-1, 0, 1}: 0 for the
-// particle's own column, else the distance to the shared face (0 if rounding put x past it).
-__device__ __forceinline__ float face_gap(float x, int c, int o, float org, float cell) {
-    if (o == 0) return 0.0f;
-    const float face = org + float(c + (o > 0 ? 1 : 0)) * cell;
-    const float g = o > 0 ? face - x : x - face;
-    return g > 0.0f ? g * g : 0.0f;
-}
-
-template <int BS>
-__global__ void __launch_bounds__(BS) k_build_nbrs_w(Dev d, Params p) {
-    constexpr int NW = BS / 32;
-    __shared__ WCell s_cell[NW][kWCells];
-    __shared__ float4 s_f[NW][kWFluid];
-    __shared__ float4 s_b[NW][kWBnd];
-    __shared__ unsigned long long s_pf, s_pb;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * BS + threadIdx.x;
-    const Scene& sc = d.scenes[block_scene(d, BS)];
-    if (threadIdx.x == 0) { s_pf = 0; s_pb = 0; }
-    const bool live = i < sc.slot_begin + sc.n;
-    const float4 xi = live ? d.pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const int cx = live ? cell_coord(xi.x, sc.ox, sc.inv_cell, sc.nx) : 0;
-    const int cy = live ? cell_coord(xi.y, sc.oy, sc.inv_cell, sc.ny) : 0;
-    const int cz = live ? cell_coord(xi.z, sc.oz, sc.inv_cell, sc.nz) : 0;
-    // the warp's box of cells (live lanes), grown by one cell and clamped to the grid
-    const int x0 = max(__reduce_min_sync(kFull, live ? cx : 0x7fffffff) - 1, 0);
-    const int y0 = max(__reduce_min_sync(kFull, live ? cy : 0x7fffffff) - 1, 0);
-    const int z0 = max(__reduce_min_sync(kFull, live ? cz : 0x7fffffff) - 1, 0);
-    const int x1 = min(__reduce_max_sync(kFull, live ? cx : -1) + 1, sc.nx - 1);
-    const int y1 = min(__reduce_max_sync(kFull, live ? cy : -1) + 1, sc.ny - 1);
-    const int z1 = min(__reduce_max_sync(kFull, live ? cz : -1) + 1, sc.nz - 1);
-    const int ex = x1 - x0 + 1, ey = y1 - y0 + 1, ez = z1 - z0 + 1;
-    const bool any_live = __any_sync(kFull, live);
-    bool staged = any_live && ex > 0 && ey > 0 && ez > 0 && ex * ey * ez <= kWCells;
-    WCell* cells = s_cell[warp];
-    if (staged) {
-        const int ncell = ex * ey * ez;
-        // cell table: lane c (and c + 32) looks up cell c of the box
-        unsigned fc[2] = {0u, 0u}, bc[2] = {0u, 0u};
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int c = lane + 32 * r;
-            if (c < ncell) {
-                const int lx = c % ex, ly = (c / ex) % ey, lz = c / (ex * ey);
-                const unsigned long long key = cell_key(sc, x0 + lx, y0 + ly, z0 + lz);
-                uint2 e;
-                const bool has = fluid_cell(d, p.slots, key, e);
-                const uint2 eb = d.btable[key];
-                fc[r] = has ? e.y - e.x : 0u;
-                bc[r] = eb.y > eb.x ? eb.y - eb.x : 0u;
-                cells[c].fstart = has ? e.x : 0u;
-                cells[c].bstart = eb.x;
-            }
-        }
-        // exclusive prefix sums of the counts over the box's cells (cell c = lane + 32 r)
-        unsigned fo[2], bo[2], ftot = 0, btot = 0;
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            unsigned f = fc[r], b = bc[r];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned tf = __shfl_up_sync(kFull, f, o), tb = __shfl_up_sync(kFull, b, o);
-                if (lane >= o) { f += tf; b += tb; }
-            }
-            fo[r] = ftot + f - fc[r];
-            bo[r] = btot + b - bc[r];
-            ftot += __shfl_sync(kFull, f, 31);
-            btot += __shfl_sync(kFull, b, 31);
-        }
-        staged = ftot <= unsigned(kWFluid) && btot <= unsigned(kWBnd);
-        if (staged) {
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const int c = lane + 32 * r;
-                if (c < ncell) {
-                    cells[c].foff = (unsigned short)fo[r];
-                    cells[c].fcnt = (unsigned short)fc[r];
-                    cells[c].boff = (unsigned short)bo[r];
-                    cells[c].bcnt = (unsigned short)bc[r];
-                }
-            }
-            __syncwarp();
-            // copy the particles: cell by cell, the warp's lanes over the cell's slots
-            for (int c = 0; c < ncell; ++c) {
-                const WCell w = cells[c];
-                for (unsigned t = lane; t < w.fcnt; t += 32) s_f[warp][w.foff + t] = d.pos[w.fstart + t];
-                for (unsigned t = lane; t < w.bcnt; t += 32) s_b[warp][w.boff + t] = d.bpos[w.bstart + t];
-            }
-        }
-        __syncwarp();
-    }
-    unsigned nf = 0, nb = 0;
-    if (live) {
-        const size_t stride = size_t(p.slots);
-        bool over = false;
-        auto fluid_test = [&](const float4& xj, unsigned j) {
-            if (j == unsigned(i)) return;
-            const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
-            const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
-            if (d2 < __fmul_rn(hij, hij)) {
-                if (nf < unsigned(p.cap_f)) d.nbr_f[size_t(nf) * stride + size_t(i)] = j; else over = true;
-                nf++;
-            }
-        };
-        auto bnd_test = [&](const float4& xj, unsigned j) {
-            const float d2 = dist2(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
-            const float hij = __fmul_rn(0.5f, __fadd_rn(xi.w, xj.w));
-            if (d2 < __fmul_rn(hij, hij)) {
-                if (nb < unsigned(p.cap_b)) d.nbr_b[size_t(nb) * stride + size_t(i)] = j; else over = true;
-                nb++;
-            }
-        };
-        const int kc = (cy & 1) | ((cz & 1) << 1);
-        const float reach = __fmul_rn(__fmul_rn(sc.cell, sc.cell), 1.001f);
-#pragma unroll 1
-        for (int t = 0; t < 27; ++t) {
-            const int code = kKeyOrder[kc][t];
-            const int ox = (code & 3) - 1, oy = ((code >> 2) & 3) - 1, oz = (code >> 4) - 1;
-            const int x = cx + ox, y = cy + oy, z = cz + oz;
-            if (x < 0 || x >= sc.nx || y < 0 || y >= sc.ny || z < 0 || z >= sc.nz) continue;
-            // a cell whose box is out of reach holds no neighbour
-            const float gap = face_gap(xi.x, cx, ox, sc.ox, sc.cell) + face_gap(xi.y, cy, oy, sc.oy, sc.cell) +
-                              face_gap(xi.z, cz, oz, sc.oz, sc.cell);
-            if (gap > reach) continue;
-            if (staged) {
-                const WCell w = cells[(x - x0) + ex * ((y - y0) + ey * (z - z0))];
-                const float4* sf = s_f[warp] + w.foff;
-                for (unsigned m = 0; m < w.fcnt; ++m) fluid_test(sf[m], w.fstart + m);
-                const float4* sb = s_b[warp] + w.boff;
-                for (unsigned m = 0; m < w.bcnt; ++m) bnd_test(sb[m], w.bstart + m);
-            } else {
-                const unsigned long long key = cell_key(sc, x, y, z);
-                uint2 e;
-                if (fluid_cell(d, p.slots, key, e)) scan_range(d.pos, e.x, e.y, fluid_test);
-                const uint2 eb = d.btable[key];
-                if (eb.x < eb.y) scan_range(d.bpos, eb.x, eb.y, bnd_test);
-            }
-        }
-        if (over) atomicOr(&d.ctr->flags, 1);
-        nf = min(nf, unsigned(p.cap_f));
-        nb = min(nb, unsigned(p.cap_b));
-    }
-    d.cnt[i] = nf | (nb << 16);
-    __syncthreads();
-    if (live) {
-        atomicAdd(&s_pf, (unsigned long long)nf);
-        atomicAdd(&s_pb, (unsigned long long)nb);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        atomicAdd(&d.ctr->fluid_pairs, s_pf);
-        atomicAdd(&d.ctr->boundary_pairs, s_pb);
-    }
-}
-
 // ------------------------------------------------------------------ boundary volume
 // V_b = 1 / (prev + W(0) + sum_k W(|x_b - x_k|)) over boundary neighbours (Akinci,
 // MPSSPHBaseUtil.cuh:10-86), with the sums and the reciprocal in float-float pairs: the volume is
@@ -1838,17 +1668,8 @@ void launch_keys(const Dev& d, const Params& p, cudaStream_t s) {
 void launch_reorder(const Dev& d, const Params& p, int n_real, cudaStream_t s) {
     if (n_real > 0) k_reorder<<<nblocks_for(n_real, 256), 256, 0, s>>>(d, p, n_real);
 }
-// 1 (default): the warp-staged search; 0: every lane scans its cells in global memory.
-#ifndef MPSG_BUILD_STAGED
-#define MPSG_BUILD_STAGED 1
-#endif
 void launch_build_nbrs(const Dev& d, const Params& p, int bs, cudaStream_t s) {
-#if MPSG_BUILD_STAGED
-    (void)bs;
-    k_build_nbrs_w<128><<<p.slots / 128, 128, 0, s>>>(d, p);
-#else
     MPSG_BS_SWITCH(bs, k_build_nbrs, d, p);
-#endif
     // neighbourhood tiles of the step's neighbour passes: built from the lists they index, so that
     // lists and tiles always change together
     if (p.stage == 1) MPSG_BS_SWITCH(bs, k_build_tiles, d, p);
