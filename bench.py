@@ -195,6 +195,9 @@ def run_ours(args, scene, rank, world, local_rank):
         st1 = sim.stats()
         # further windows of the same length continuing the run (spread of the figure, and more
         # clock samples under load); `value` is the first window's
+        # (the windows differ in work: the scene evolves, and so do the solvers' iteration counts)
+        win_iters = []
+        prev = st1
         for _ in range(args.repeats):
             r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             r0.record(stream)
@@ -202,6 +205,9 @@ def run_ours(args, scene, rank, world, local_rank):
             r1.record(stream)
             r1.synchronize()
             repeat_ms.append(r0.elapsed_time(r1) / args.steps)
+            cur = sim.stats()
+            win_iters.append([(cur["iters_total"][k] - prev["iters_total"][k]) / args.steps for k in range(3)])
+            prev = cur
     torch.cuda.synchronize(dev)
     t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if dist:
@@ -273,6 +279,7 @@ def run_ours(args, scene, rank, world, local_rank):
         "iterations_per_step": {"df": iters[0] / args.steps, "cg": iters[1] / args.steps, "cd": iters[2] / args.steps},
         "windows": {"ms_per_step": [ms_max / args.steps] + repeat_ms,
                     "median_ms_per_step": statistics.median([ms_max / args.steps] + repeat_ms),
+                    "iterations_per_step_df_cg_cd": [[iters[k] / args.steps for k in range(3)]] + win_iters,
                     "note": "the timed window, then %d more windows of %d steps continuing the run" %
                             (len(repeat_ms), args.steps)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -69,43 +69,49 @@ __device__ void emit_line(V3 a, V3 b, float d, Emit& e) {
     }
 }
 
-// Counts (out == null) or writes the samples of face f.
+// Counts (out == null) or writes the samples of face f: the corners and edges the face owns
+// (bits 0-2 and 3-5 of rtri[f]), then a sweep of lines parallel to the face's shortest edge,
+// stepping both ends along the two other edges.  The steps are the reference's
+// (MPSParticleSamplingUtil.cuh:69-240), so that a mesh gives the same boundary particles: the
+// parity test of mps_mesh_sample compares count and points with the reference's own sampler.
 __device__ unsigned sample_face(const double* V, const unsigned* F, const unsigned* rtri, unsigned f, double R,
                                 float4* out, unsigned* face_id, unsigned at, unsigned end) {
-    V3 ns[3];
+    V3 corner[3];
     for (int k = 0; k < 3; ++k) {
         const unsigned v = F[3 * f + k];
-        ns[k] = V3{V[3 * v], V[3 * v + 1], V[3 * v + 2]};
+        corner[k] = V3{V[3 * v], V[3 * v + 1], V[3 * v + 2]};
     }
-    V3 es[3] = {sub(ns[1], ns[0]), sub(ns[2], ns[1]), sub(ns[0], ns[2])};
-    const double ls[3] = {len(es[0]), len(es[1]), len(es[2])};
-    unsigned s = 0u;
-    if (ls[s] > ls[1]) s = 1u;
-    if (ls[s] > ls[2]) s = 2u;
-    const double d = (R + R) * 0.25;
-    const unsigned info = rtri[f];
+    V3 edge[3] = {sub(corner[1], corner[0]), sub(corner[2], corner[1]), sub(corner[0], corner[2])};
+    const double elen[3] = {len(edge[0]), len(edge[1]), len(edge[2])};
+    unsigned shortest = 0u;
+    if (elen[shortest] > elen[1]) shortest = 1u;
+    if (elen[shortest] > elen[2]) shortest = 2u;
+    const double spacing = (R + R) * 0.25;
+    const unsigned owned = rtri[f];
     Emit e{out, face_id, at, end, float(R * 0.25), f};
-    for (unsigned i = 0; i < 3u; ++i) {
-        if ((info >> i) & 1u) e.put(ns[i]);
-        if ((info >> (i + 3u)) & 1u) {
-            if (out) emit_line(ns[i], ns[(i + 1u) % 3u], float(d), e);
-            else e.at += line_points(ls[i], d);
+    for (unsigned c = 0; c < 3u; ++c) {
+        if ((owned >> c) & 1u) e.put(corner[c]);
+        if ((owned >> (c + 3u)) & 1u) {
+            if (out) emit_line(corner[c], corner[(c + 1u) % 3u], float(spacing), e);
+            else e.at += line_points(elen[c], spacing);
         }
     }
-    const unsigned i0 = (s + 1u) % 3u, i1 = (s + 2u) % 3u;
-    ns[i1] = ns[s];
-    const V3 c = cross(es[s], cross(es[s], es[i1]));
-    const V3 dir = mul(c, 1.0 / sqrt(dot(c, c)));
-    es[i1] = mul(es[i1], -1.0);
-    const double l = dot(dir, es[i0]);
-    const unsigned nt = line_points(l, d);
-    if (nt > 0u) {
-        const double stride = (l / double(nt + 1u)) / l;
-        for (unsigned k = 0; k < nt; ++k) {
-            ns[i0] = add(ns[i0], mul(es[i0], stride));
-            ns[i1] = add(ns[i1], mul(es[i1], stride));
-            if (out) emit_line(ns[i0], ns[i1], float(d), e);
-            else e.at += line_points(len(sub(ns[i0], ns[i1])), d);
+    // sweep: end A walks edge `ea` from its start, end B walks the reversed edge `eb` from the
+    // shortest edge's start (both edges meet the shortest one's far corner)
+    const unsigned ea = (shortest + 1u) % 3u, eb = (shortest + 2u) % 3u;
+    V3 endA = corner[ea], endB = corner[shortest];
+    const V3 normal_in_plane = cross(edge[shortest], cross(edge[shortest], edge[eb]));
+    const V3 across = mul(normal_in_plane, 1.0 / sqrt(dot(normal_in_plane, normal_in_plane)));
+    const V3 stepB = mul(edge[eb], -1.0);
+    const double height = dot(across, edge[ea]);
+    const unsigned rows = line_points(height, spacing);
+    if (rows > 0u) {
+        const double frac = (height / double(rows + 1u)) / height;
+        for (unsigned r = 0; r < rows; ++r) {
+            endA = add(endA, mul(edge[ea], frac));
+            endB = add(endB, mul(stepB, frac));
+            if (out) emit_line(endA, endB, float(spacing), e);
+            else e.at += line_points(len(sub(endA, endB)), spacing);
         }
     }
     return e.at - at;
