@@ -21,7 +21,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -111,11 +110,7 @@ class ClockSampler:
 
 
 def radix_passes(sim) -> int:
-    g = sim.grid()
-    nx, ny, nz = g["dims"]
-    cells = nx * (ny + ny % 2) * (nz + nz % 2)  # key space: ny, nz padded to whole 2 x 2 columns
-    bits = max(1, math.ceil(math.log2(max(2, cells))))
-    return math.ceil(bits / 8)
+    return int(sim.stats()["sort_passes"])
 
 
 def workload_config(scene, world: int = 1) -> dict:
@@ -324,6 +319,7 @@ def run_batched(args, scenes_list, rank, world, local_rank):
     sim = BatchedSimulation(local, device=local_rank, **best)
     sim.step(args.warmup, stream)
     torch.cuda.synchronize(dev)
+    st0 = sim.stats()
     if dist:
         import torch.distributed as td
         td.barrier()
@@ -334,6 +330,11 @@ def run_batched(args, scenes_list, rank, world, local_rank):
         e1.record(stream)
         e1.synchronize()
     ms = e0.elapsed_time(e1)
+    st1 = sim.stats()
+    passes = [st1["passes_total"][k] - st0["passes_total"][k] for k in range(3)]
+    P = radix_passes(sim)
+    static = sim.launches_per_step((0, 0, 0), P)
+    launches = args.steps * static + sim.launches_per_step(tuple(passes), P) - static
     t = torch.tensor([ms], dtype=torch.float64, device=dev)
     tot = torch.tensor([n_local], dtype=torch.float64, device=dev)
     if dist:
@@ -369,6 +370,7 @@ def run_batched(args, scenes_list, rank, world, local_rank):
         "autotuned": {"best": best, "ms_per_step": {f"bs{c['block_size']}_d{c['sort_digit_bits']}": round(ms, 3)
                                                     for ms, c in tuned}},
         "max_iterations": {"df": int(its[:, 0].max()), "cg": int(its[:, 1].max()), "cd": int(its[:, 2].max())},
+        "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if dist:

@@ -128,6 +128,7 @@ typedef struct mps_stats {
                               * return at once) */
     int64_t tile_blocks[2];  /* stage 1: blocks of the last neighbour build with a neighbourhood tile,
                               * and blocks whose neighbourhood exceeded the tile (global gathers) */
+    int64_t sort_passes;     /* radix passes of the step's cell sort (significant key bits / digit) */
 } mps_stats;
 
 typedef struct mps_handle mps_handle;

@@ -58,7 +58,8 @@ class Stats(C.Structure):
     _fields_ = [("df_iters", C.c_int32), ("cg_iters", C.c_int32), ("cd_iters", C.c_int32), ("flags", C.c_int32),
                 ("df_err", C.c_double), ("cd_err", C.c_double), ("cg_rr", C.c_double), ("fluid_pairs", C.c_int64),
                 ("boundary_pairs", C.c_int64), ("steps", C.c_int64), ("iters_total", C.c_int64 * 3),
-                ("runs_total", C.c_int64 * 3), ("passes_total", C.c_int64 * 3), ("tile_blocks", C.c_int64 * 2)]
+                ("runs_total", C.c_int64 * 3), ("passes_total", C.c_int64 * 3), ("tile_blocks", C.c_int64 * 2),
+                ("sort_passes", C.c_int64)]
 
 
 EXPORTS = {

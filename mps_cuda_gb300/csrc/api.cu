@@ -1031,6 +1031,7 @@ int mps_get_stats(mps_handle* h, mps_stats* out, void* stream) {
     out->tile_blocks[0] = int64_t(c.tile_blocks[0]);
     out->tile_blocks[1] = int64_t(c.tile_blocks[1]);
     out->steps = h->steps;
+    out->sort_passes = (h->key_bits + h->cfg.sort_digit_bits - 1) / h->cfg.sort_digit_bits;
     for (int k = 0; k < 3; ++k) {
         out->iters_total[k] = int64_t(c.iters_total[k]);
         out->runs_total[k] = int64_t(c.runs_total[k]);

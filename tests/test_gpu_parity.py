@@ -81,6 +81,10 @@ def test_sort_keys_and_ranges_bit_exact(mps, orc):
     assert np.array_equal(gpu_ids, order)
     # positions were moved with their particles
     assert np.array_equal(sim.get_field("pos", order="id")[:, :3], sc.pos4[:, :3])
+    # the sort processes the significant bits of the scene's key space (2 x 2 columns: ny, nz even)
+    nx, ny, nz = g["dims"]
+    bits = max(1, int(nx * (ny + ny % 2) * (nz + nz % 2) - 1).bit_length())
+    assert sim.stats()["sort_passes"] == -(-bits // sim.cfg.sort_digit_bits)
 
 
 def test_neighbour_counts_bit_exact(mps, orc, small):
