@@ -367,7 +367,7 @@ def run_batched(args, scenes_list, rank, world, local_rank):
                    "boundary_particles": sum(s.nb for s in scenes_list), "parallelism": "scenes split over ranks"},
         "per_scene_launches": {"value": per_value, "unit": UNIT, "ms_for_all_scenes_one_step": per_ms},
         "batched_over_per_scene": value / per_value,
-        "autotuned": {"best": best, "ms_per_step": {f"bs{c['block_size']}_d{c['sort_digit_bits']}": round(ms, 3)
+        "autotuned": {"best": best, "ms_per_step": {f"bs{c['block_size']}_d{c['sort_digit_bits']}_u{c.get('cg_unroll', 4)}": round(ms, 3)
                                                     for ms, c in tuned}},
         "max_iterations": {"df": int(its[:, 0].max()), "cg": int(its[:, 1].max()), "cd": int(its[:, 2].max())},
         "gpu_launches": launches,

@@ -89,12 +89,17 @@ typedef struct mps_config {
     int32_t sort_digit_bits;     /* radix digit width of the cell sort (1..8) */
     int32_t visc_solver;         /* mps_visc_solver: implicit viscosity/surface-tension solve */
     int32_t cg_form;             /* mps_cg_form: arrangement of the CG iteration (same iterates) */
+    int32_t cg_unroll;           /* CG iterations per body of the device-side loop (1..8, default 4): the
+                                    iterations after the stop return at once, so more save loop
+                                    evaluations and fewer save empty launches; results do not change */
 } mps_config;
 
-/* MPS_CG_THREE_PASS (default): the reference's arrangement (MPSSolver.cuh:33-60): A p with r.r
- * and p.Ap, then x/r update with the new r.r, then the direction update.  MPS_CG_TWO_PASS: the
- * Chronopoulos-Gear arrangement: A r with r.r and r.w, then one vector pass updating p, s = A p
- * (by recurrence), x and r; about 5 % faster per step.  Equal in exact arithmetic; in FP32 the
+/* MPS_CG_THREE_PASS (default): the reference's iteration (MPSSolver.cuh:33-60) in three
+ * launches: A p with r.r, p.Ap, r.Ap and Ap.Ap; the decision (stop test on r.r, alpha = r.r / p.Ap,
+ * beta = (r.r - 2 alpha r.Ap + alpha^2 Ap.Ap) / r.r, the new r.r expanded); one vector pass
+ * x += alpha p, r -= alpha Ap, p = r + beta p.  MPS_CG_TWO_PASS: the Chronopoulos-Gear
+ * arrangement: A r with r.r and r.w, then one vector pass updating p, s = A p (by recurrence), x
+ * and r.  Equal in exact arithmetic; in FP32 the
  * recurrence for s adds rounding: against the FP64 oracle from an identical state, single
  * particles' velocities then differ by up to ~1e-4 (max-norm) where the three-pass form stays
  * below ~3e-6 (RMS ~2e-7 for both). */

@@ -51,7 +51,7 @@ class Config(C.Structure):
                 ("cg_factor", C.c_double), ("fixed_iters", C.c_int32), ("max_fluid_neighbors", C.c_int32),
                 ("max_boundary_neighbors", C.c_int32), ("volume_accumulate", C.c_int32), ("use_graph", C.c_int32),
                 ("block_size", C.c_int32), ("stage", C.c_int32), ("sort_digit_bits", C.c_int32),
-                ("visc_solver", C.c_int32), ("cg_form", C.c_int32)]
+                ("visc_solver", C.c_int32), ("cg_form", C.c_int32), ("cg_unroll", C.c_int32)]
 
 
 class Stats(C.Structure):

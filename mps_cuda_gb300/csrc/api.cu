@@ -78,7 +78,7 @@ void mps_handle::release() {
     void** ptrs[] = {(void**)&pos[0], (void**)&pos[1], (void**)&vel[0], (void**)&vel[1], (void**)&ids[0],
                      (void**)&ids[1], (void**)&slot_key, (void**)&ftable, (void**)&btable, (void**)&d_scenes,
                      (void**)&chunk_scene, (void**)&nbr_f, (void**)&nbr_b, (void**)&cnt, (void**)&rho, (void**)&rdev,
-                     (void**)&alpha, (void**)&kappa, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
+                     (void**)&alpha, (void**)&kappa, (void**)&xk, (void**)&delta, (void**)&aux, (void**)&color, (void**)&cg_x,
                      (void**)&cg_r, (void**)&cg_p, (void**)&cg_ap, (void**)&cg_b, (void**)&cg_s, (void**)&cg_coef,
                      (void**)&bpos, (void**)&bvol, (void**)&bvol_lo,
                      (void**)&partial, (void**)&acc, (void**)&nbr_t, (void**)&tile_j, (void**)&tile_n, (void**)&solve, (void**)&ctr, (void**)&scene_iters, (void**)&scene_err,
@@ -164,6 +164,7 @@ Dev make_dev(const mps_handle* h, int sorted_buf) {
     d.rho = h->rho;
     d.alpha = h->alpha;
     d.kappa = h->kappa;
+    d.xk = h->xk;
     d.delta = h->delta;
     d.rdev = h->rdev;
     d.aux = h->aux;
@@ -288,6 +289,8 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->rho, S));
     MPS_CUDA_TRY(dalloc(&h->alpha, S));
     MPS_CUDA_TRY(dalloc(&h->kappa, S));
+    MPS_CUDA_TRY(dalloc(&h->xk, S));
+    MPS_CUDA_TRY(cudaMemset(h->xk, 0, S * sizeof(float4)));
     MPS_CUDA_TRY(dalloc(&h->delta, S));
     MPS_CUDA_TRY(dalloc(&h->rdev, S));
     MPS_CUDA_TRY(dalloc(&h->aux, S));
@@ -304,7 +307,7 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->bpos, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->bvol, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->bvol_lo, size_t(std::max<int64_t>(h->nb, 1))));
-    MPS_CUDA_TRY(dalloc(&h->partial, 2 * (S / 64 + 1)));
+    MPS_CUDA_TRY(dalloc(&h->partial, 4 * (S / 64 + 1)));   // up to 32 bytes a 64-slot block
     // the loop-sum accumulators start at zero; each decide kernel zeroes what it has read (one
     // region more than the scenes: the profiling forms of the pass kernels add into it, unread)
     const size_t acc_words = (size_t(h->nscenes) + 1) * kAccLanes * kAccStride;
@@ -418,8 +421,7 @@ int eager_loop(mps_handle* h, cudaStream_t s, int kind /*0 DF,1 CG,2 CD*/) {
             launch_cg_update(d, p, bs, 0ull, 0, 0, s);
         } else if (kind == 1) {
             launch_cg_ap3(d, p, bs, 0ull, 0, s);
-            launch_cg_update3(d, p, bs, s);
-            launch_cg_dir3(d, p, bs, 0ull, 0, 0, s);
+            launch_cg_vec3(d, p, bs, 0ull, 0, 0, s);
         } else {
             launch_pressure_A(d, p, kind == 0 ? 0 : 1, bs, 0ull, 0, s);
             launch_pressure_B(d, p, bs, 0ull, 0, 0, s);
@@ -470,13 +472,10 @@ int run_phase(mps_handle* h, int phase, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ graph capture
-// CG passes per WHILE body.  Each pass's kernels return at once when its scene has stopped, so
-// a body may hold several passes: fewer conditional evaluations (about 3.6 us each on the 1M
-// step) against up to MPSG_CG_UNROLL - 1 empty passes after the stop (1M step: 7.08 ms with 1,
-// 7.02 with 2, 6.99 with 4).
-#ifndef MPSG_CG_UNROLL
-#define MPSG_CG_UNROLL 4
-#endif
+// CG passes per WHILE body (mps_config.cg_unroll).  Each pass's kernels return at once when its
+// scene has stopped, so a body may hold several passes: fewer conditional evaluations (about
+// 3.6 us each on the 1M step) against up to cg_unroll - 1 empty passes after the stop (1M step:
+// 7.08 ms with 1, 7.02 with 2, 6.99 with 4).
 
 // Hard bound on the passes of one device-side solve (kind 0 DF, 1 CG, 2 CD): the decision logic
 // ends a loop after at most the iteration cap, and a CG body runs on to its last pass (the cap
@@ -484,7 +483,7 @@ int run_phase(mps_handle* h, int phase, cudaStream_t s) {
 // decision logic failed, and flags the step (bit 2).
 int loop_limit(const mps_handle* h, int kind) {
     const int cap = h->cfg.fixed_iters > 0 ? h->cfg.fixed_iters : (kind == 1 ? h->cfg.cg_max_iter : h->cfg.max_iter);
-    const int u = kind == 1 ? MPSG_CG_UNROLL : 1;
+    const int u = kind == 1 ? h->cfg.cg_unroll : 1;
     return (cap + u - 1) / u * u + 2;
 }
 
@@ -591,7 +590,7 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
         {
             Capture b{body, h->cap_stream, {}};
             MPS_CAP_TRY(seg_begin(b));
-            for (int u = 0; u < MPSG_CG_UNROLL; ++u) {
+            for (int u = 0; u < h->cfg.cg_unroll; ++u) {
                 if (p.visc_solver) {
                     launch_jacobi(d, p, bs, hcg, 1, loop_limit(h, 1), nullptr, nullptr, b.s);
                 } else if (p.cg_form == 1) {
@@ -599,8 +598,7 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
                     launch_cg_update(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
                 } else {
                     launch_cg_ap3(d, p, bs, hcg, 1, b.s);
-                    launch_cg_update3(d, p, bs, b.s);
-                    launch_cg_dir3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+                    launch_cg_vec3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
                 }
             }
             MPS_CAP_TRY(cudaGetLastError());
@@ -765,6 +763,7 @@ void mps_default_config(mps_config* c) {
     c->sort_digit_bits = 8;
     c->visc_solver = MPS_VISC_CG;
     c->cg_form = MPS_CG_THREE_PASS;
+    c->cg_unroll = 4;
 }
 
 // SPHMaterial() + SetRadius(h): V = h^3 / 48 * 3.141592, mass = density * V
@@ -802,6 +801,7 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;
     if (h->cfg.visc_solver != MPS_VISC_JACOBI) h->cfg.visc_solver = MPS_VISC_CG;
     if (h->cfg.cg_form != MPS_CG_TWO_PASS) h->cfg.cg_form = MPS_CG_THREE_PASS;
+    if (h->cfg.cg_unroll < 1 || h->cfg.cg_unroll > 8) h->cfg.cg_unroll = 4;
     if (h->cfg.stage != 1) h->cfg.stage = 0;
     *out = h;
     return MPS_OK;

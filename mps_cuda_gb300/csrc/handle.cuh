@@ -51,6 +51,7 @@ struct mps_handle {
     unsigned* nbr_b = nullptr;
     unsigned* cnt = nullptr;
     float *rho = nullptr, *rdev = nullptr, *alpha = nullptr, *kappa = nullptr, *delta = nullptr;
+    float4* xk = nullptr;
     float2* aux = nullptr;
     float4* color = nullptr;
     float4 *cg_x = nullptr, *cg_r = nullptr, *cg_p = nullptr, *cg_ap = nullptr, *cg_b = nullptr, *cg_s = nullptr;

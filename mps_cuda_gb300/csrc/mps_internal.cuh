@@ -79,7 +79,7 @@ struct StepCounters {
     unsigned long long tile_blocks[2];  // neighbourhood tiles of the step: blocks with a tile, blocks without
     unsigned long long iters_total[3];  // sum over steps and scenes of the loop counter (DF, CG, CD)
     unsigned long long runs_total[3];   // solver passes that ran (one per iteration; max over scenes)
-    unsigned long long passes_total[3]; // solver passes launched (a graph body holds MPSG_CG_UNROLL CG passes)
+    unsigned long long passes_total[3]; // solver passes launched (a graph body holds cg_unroll CG passes)
 };
 
 // Uniform parameters, passed by value to every kernel.
@@ -132,6 +132,7 @@ struct Dev {
     float* rdev;                  // rho / rho0 - 1 from the compensated sums (the stiffness reads this)
     float* alpha;
     float* kappa;
+    float4* xk;                   // (x, y, z, kappa) of each slot from pressure pass A, gathered by pass B
     float* delta;
     float2* aux;                  // (rho, st factor) packed for the CG gathers
     float4* color;
@@ -489,11 +490,11 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long 
                       cudaStream_t s);
 // three-pass form: A p + dots, x/r update + r.r, direction update (with the loop guard)
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s);
-void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s);
-// The three-pass update and direction passes in their profiling form (no loop decision).
-void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s);
-void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+// The three-pass CG's vector pass (x, r and p in one sweep), and its profiling form (no loop
+// decision).
+void launch_cg_vec3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s);
+void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s);
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);
 // Jacobi sweep of the viscosity/surface-tension system; src/dst null = the two iterate buffers
 // chosen by the scene's loop counter (graph form), else explicit (adjoint recording).
