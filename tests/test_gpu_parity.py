@@ -307,6 +307,25 @@ def test_graph_with_cg_cap_equals_host_loop(mps, form):
     assert np.array_equal(pg, pe) and np.array_equal(vg, ve)
 
 
+@pytest.mark.parametrize("unroll", [1, 3, 8])
+def test_cg_unroll_changes_nothing(mps, unroll):
+    """CG iterations per device-loop body (the autotuner's cg_unroll): the iterations after the
+    stop return at once, so every value gives the same bits as the default, with the cap reached
+    inside a body and with an adaptive stop."""
+    from mps_cuda_gb300 import Simulation, scenes
+    sc = scenes.dam_break_small(10, seed=9)
+    for extra in ({}, {"cg_max_iter": 5}):
+        ref = Simulation.from_scene(sc, **extra)
+        sim = Simulation.from_scene(sc, cg_unroll=unroll, **extra)
+        ref.step(3)
+        sim.step(3)
+        assert sim.stats()["cg_iters"] == ref.stats()["cg_iters"]
+        assert sim.stats()["iters_total"] == ref.stats()["iters_total"]
+        pr, vr = ref.get_fluid()
+        ps, vs = sim.get_fluid()
+        assert np.array_equal(pr, ps) and np.array_equal(vr, vs)
+
+
 def test_overflow_and_nonfinite_are_reported(mps):
     from mps_cuda_gb300 import MpsError, Simulation, scenes
     sc = scenes.dam_break_small(6, seed=1)
