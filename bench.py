@@ -640,14 +640,29 @@ def _step_vs_oracle(sim, o, scene, mps, orc, sim1=None, o1=None):
                 "density_rms_rel": float(np.sqrt(np.mean((rg - ro) ** 2)) / rho0),
                 "alpha_max_rel": float(np.abs(ag - ao).max() / np.abs(ao).max())})
     for gph, oph, name in ((mps.PHASE_DF, orc.DF, "df"), (mps.PHASE_VISCST, orc.VISCST, "cg"), (mps.PHASE_CD, orc.CD, "cd")):
-        o.put("vel", sim.get_field("vel")[:, :3].astype(np.float64))   # each solve from the same state
+        v_in = sim.get_field("vel")[:, :3].astype(np.float64)
+        o.put("vel", v_in)   # each solve from the same state
         sim.phase(gph)
         o.phase(oph)
         vg, vo = sim.get_field("vel")[:, :3].astype(np.float64), o.get("vel")
         out[f"velocity_after_{name}_max_rel"] = float(np.abs(vg - vo).max() / np.abs(vo).max())
+        if name == "cg":
+            ig, io = sim.stats()["cg_iters"], o.stats()["cg_iters"]
+            cg_iters_oracle = io
+            out["cg_rr_final_gpu_oracle_tol"] = [sim.stats()["cg_rr"], o.stats()["cg_rr"], float(sim.cfg.cg_tol)]
+            if ig != io and ig > 1:
+                # the adaptive stop (r.r < tol) fell on different iterations: the same solve on the
+                # oracle with the GPU's number of updates (the loop counter minus one), from the same state
+                o.put("vel", v_in)
+                o.set_fixed_iters(ig - 1)
+                o.phase(oph)
+                o.set_fixed_iters(0)
+                vo2 = o.get("vel")
+                out["velocity_after_cg_same_updates_max_rel"] = float(np.abs(vg - vo2).max() / np.abs(vo2).max())
+                o.put("vel", vo)
     st, so = sim.stats(), o.stats()
     out["iters_gpu"] = [st["df_iters"], st["cg_iters"], st["cd_iters"]]
-    out["iters_oracle"] = [so["df_iters"], so["cg_iters"], so["cd_iters"]]
+    out["iters_oracle"] = [so["df_iters"], cg_iters_oracle, so["cd_iters"]]   # (the adaptive CG's count)
     kg, ko = sim.get_field("pressure").astype(np.float64), o.get("pressure")
     out["pressure_max_rel"] = float(np.abs(kg - ko).max() / max(np.abs(ko).max(), 1e-30))
     out["pressure_rms_rel"] = float(np.sqrt(np.mean((kg - ko) ** 2)) / max(np.sqrt(np.mean(ko ** 2)), 1e-30))

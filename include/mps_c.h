@@ -94,12 +94,10 @@ typedef struct mps_config {
                                     evaluations and fewer save empty launches; results do not change */
 } mps_config;
 
-/* MPS_CG_THREE_PASS (default): the reference's iteration (MPSSolver.cuh:33-60) in three
- * launches: A p with r.r, p.Ap, r.Ap and Ap.Ap; the decision (stop test on r.r, alpha = r.r / p.Ap,
- * beta = (r.r - 2 alpha r.Ap + alpha^2 Ap.Ap) / r.r, the new r.r expanded); one vector pass
- * x += alpha p, r -= alpha Ap, p = r + beta p.  MPS_CG_TWO_PASS: the Chronopoulos-Gear
- * arrangement: A r with r.r and r.w, then one vector pass updating p, s = A p (by recurrence), x
- * and r.  Equal in exact arithmetic; in FP32 the
+/* MPS_CG_THREE_PASS (default): the reference's arrangement (MPSSolver.cuh:33-60): A p with r.r
+ * and p.Ap, then the r update with the new r.r, then x and the direction.  MPS_CG_TWO_PASS: the
+ * Chronopoulos-Gear arrangement: A r with r.r and r.w, then one vector pass updating p, s = A p
+ * (by recurrence), x and r.  Equal in exact arithmetic; in FP32 the
  * recurrence for s adds rounding: against the FP64 oracle from an identical state, single
  * particles' velocities then differ by up to ~1e-4 (max-norm) where the three-pass form stays
  * below ~3e-6 (RMS ~2e-7 for both). */

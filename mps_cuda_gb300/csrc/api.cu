@@ -307,7 +307,7 @@ int allocate(mps_handle* h) {
     MPS_CUDA_TRY(dalloc(&h->bpos, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->bvol, size_t(std::max<int64_t>(h->nb, 1))));
     MPS_CUDA_TRY(dalloc(&h->bvol_lo, size_t(std::max<int64_t>(h->nb, 1))));
-    MPS_CUDA_TRY(dalloc(&h->partial, 4 * (S / 64 + 1)));   // up to 32 bytes a 64-slot block
+    MPS_CUDA_TRY(dalloc(&h->partial, 2 * (S / 64 + 1)));
     // the loop-sum accumulators start at zero; each decide kernel zeroes what it has read (one
     // region more than the scenes: the profiling forms of the pass kernels add into it, unread)
     const size_t acc_words = (size_t(h->nscenes) + 1) * kAccLanes * kAccStride;
@@ -421,7 +421,8 @@ int eager_loop(mps_handle* h, cudaStream_t s, int kind /*0 DF,1 CG,2 CD*/) {
             launch_cg_update(d, p, bs, 0ull, 0, 0, s);
         } else if (kind == 1) {
             launch_cg_ap3(d, p, bs, 0ull, 0, s);
-            launch_cg_vec3(d, p, bs, 0ull, 0, 0, s);
+            launch_cg_update3(d, p, bs, s);
+            launch_cg_dir3(d, p, bs, 0ull, 0, 0, s);
         } else {
             launch_pressure_A(d, p, kind == 0 ? 0 : 1, bs, 0ull, 0, s);
             launch_pressure_B(d, p, bs, 0ull, 0, 0, s);
@@ -598,7 +599,8 @@ cudaError_t capture_steps(mps_handle* h, cudaGraph_t g, int cur, int nsteps) {
                     launch_cg_update(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
                 } else {
                     launch_cg_ap3(d, p, bs, hcg, 1, b.s);
-                    launch_cg_vec3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
+                    launch_cg_update3(d, p, bs, b.s);
+                    launch_cg_dir3(d, p, bs, hcg, 1, loop_limit(h, 1), b.s);
                 }
             }
             MPS_CAP_TRY(cudaGetLastError());

@@ -490,11 +490,11 @@ void launch_cg_update(const Dev& d, const Params& p, int bs, unsigned long long 
                       cudaStream_t s);
 // three-pass form: A p + dots, x/r update + r.r, direction update (with the loop guard)
 void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, cudaStream_t s);
-// The three-pass CG's vector pass (x, r and p in one sweep), and its profiling form (no loop
-// decision).
-void launch_cg_vec3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
-                    cudaStream_t s);
+void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s);
+// The three-pass update and direction passes in their profiling form (no loop decision).
 void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s);
+void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+                    cudaStream_t s);
 void launch_cg_finish(const Dev& d, const Params& p, cudaStream_t s);
 // Jacobi sweep of the viscosity/surface-tension system; src/dst null = the two iterate buffers
 // chosen by the scene's loop counter (graph form), else explicit (adjoint recording).

@@ -15,7 +15,7 @@
 //   k_st_factor, k_cg_*    ComputeSurfaceTensionFactor/CGb/CGAp, ComputeCGViscosityAp,
 //                          ComputeFinalCGAp (MPSSPHNonPressureUtil.cuh:425-648) and CGSolver
 //                          (MPSSolver.cuh:12-73, MPSCGKernel.cuh:5-133) with device-side dots
-//                          (k_cg_decide3 / k_cg_decide2: the solver's scalars).
+//                          (k_cg_decide3 / k_cg_beta3 / k_cg_decide2: the solver's scalars).
 //   k_advect               BoundaryCollision + UpdatePosition (MPSAdvectUtil.cuh:36-77).
 #include "mps_internal.cuh"
 
@@ -136,38 +136,30 @@ __device__ __forceinline__ void put_partial(const Dev& d, int b, double v0, doub
     const float2 a = df_from(v0), c = df_from(v1);
     reinterpret_cast<float4*>(d.partial)[b] = make_float4(a.x, a.y, c.x, c.y);
 }
-// Block sums of four per-thread FP32 values stored as block b's partials (32 bytes a block):
-// FP32 within a warp, then the warps' sums added by thread 0 as compensated FP32 pairs (TwoSum:
-// the pair holds the exact sum of the warp sums to about 48 bits), with no FP64 arithmetic at the
-// end of the block.  sh: BS / 32 entries.
+// Block sums of two per-thread FP32 values stored as block b's partials (16 bytes a block, the
+// layout of put_partial): FP32 within a warp, then the warps' sums added by thread 0 as
+// compensated FP32 pairs (TwoSum: each pair holds the exact sum of the warp sums to about 48
+// bits), with no FP64 arithmetic at the end of the block (1M CG operator pass: 112 -> 110 us
+// against FP64 block sums).  sh: BS / 32 entries.
 template <int BS>
-__device__ __forceinline__ void block_partial4(const Dev& d, float a, float b, float c, float e, float4* sh) {
+__device__ __forceinline__ void block_partial2(const Dev& d, float a, float b, float2* sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(kFull, a, o);
         b += __shfl_down_sync(kFull, b, o);
-        c += __shfl_down_sync(kFull, c, o);
-        e += __shfl_down_sync(kFull, e, o);
     }
     __syncthreads();
-    if (lane == 0) sh[warp] = make_float4(a, b, c, e);
+    if (lane == 0) sh[warp] = make_float2(a, b);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const float4 w0 = sh[0];
-        float2 t0 = make_float2(w0.x, 0.f), t1 = make_float2(w0.y, 0.f), t2 = make_float2(w0.z, 0.f),
-               t3 = make_float2(w0.w, 0.f);
+        float2 t0 = make_float2(sh[0].x, 0.f), t1 = make_float2(sh[0].y, 0.f);
 #pragma unroll
         for (int w = 1; w < BS / 32; ++w) {
-            const float4 v = sh[w];
-            t0 = df_add(t0, make_float2(v.x, 0.f));
-            t1 = df_add(t1, make_float2(v.y, 0.f));
-            t2 = df_add(t2, make_float2(v.z, 0.f));
-            t3 = df_add(t3, make_float2(v.w, 0.f));
+            t0 = df_add(t0, make_float2(sh[w].x, 0.f));
+            t1 = df_add(t1, make_float2(sh[w].y, 0.f));
         }
-        float4* P = reinterpret_cast<float4*>(d.partial) + 2 * size_t(blockIdx.x);
-        P[0] = make_float4(t0.x, t0.y, t1.x, t1.y);
-        P[1] = make_float4(t2.x, t2.y, t3.x, t3.y);
+        reinterpret_cast<float4*>(d.partial)[blockIdx.x] = make_float4(t0.x, t0.y, t1.x, t1.y);
     }
 }
 
@@ -359,73 +351,6 @@ __device__ double2 scene_partials(const Dev& d, const Scene& sc, int spb, double
         }
     }
     return make_double2(df_to(tx), NC == 2 ? df_to(ty) : 0.0);   // valid in thread 0
-}
-// The same for four components stored by put_partial4 (sh: 2 * NT / 32 float4); the sums land in
-// out[0..3] of thread 0.
-template <int NT>
-__device__ void scene_partials4(const Dev& d, const Scene& sc, int spb, float4* sh, double* out) {
-    const int b0 = sc.slot_begin / spb, b1 = sc.slot_end / spb;
-    const float4* P = reinterpret_cast<const float4*>(d.partial);
-    float2 acc[kSumILP][4];
-#pragma unroll
-    for (int u = 0; u < kSumILP; ++u)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[u][c] = make_float2(0.f, 0.f);
-    int b = b0 + int(threadIdx.x);
-    for (; b + (kSumILP - 1) * NT < b1; b += kSumILP * NT) {
-        float4 v[kSumILP][2];
-#pragma unroll
-        for (int u = 0; u < kSumILP; ++u) {
-            v[u][0] = __ldcg(P + 2 * size_t(b + u * NT));
-            v[u][1] = __ldcg(P + 2 * size_t(b + u * NT) + 1);
-        }
-#pragma unroll
-        for (int u = 0; u < kSumILP; ++u) {
-            acc[u][0] = df_add(acc[u][0], make_float2(v[u][0].x, v[u][0].y));
-            acc[u][1] = df_add(acc[u][1], make_float2(v[u][0].z, v[u][0].w));
-            acc[u][2] = df_add(acc[u][2], make_float2(v[u][1].x, v[u][1].y));
-            acc[u][3] = df_add(acc[u][3], make_float2(v[u][1].z, v[u][1].w));
-        }
-    }
-    for (; b < b1; b += NT) {
-        const float4 v0 = __ldcg(P + 2 * size_t(b)), v1 = __ldcg(P + 2 * size_t(b) + 1);
-        acc[0][0] = df_add(acc[0][0], make_float2(v0.x, v0.y));
-        acc[0][1] = df_add(acc[0][1], make_float2(v0.z, v0.w));
-        acc[0][2] = df_add(acc[0][2], make_float2(v1.x, v1.y));
-        acc[0][3] = df_add(acc[0][3], make_float2(v1.z, v1.w));
-    }
-    float2 t[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        t[c] = acc[0][c];
-#pragma unroll
-        for (int u = 1; u < kSumILP; ++u) t[c] = df_add(t[c], acc[u][c]);
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-            t[c] = df_add(t[c], make_float2(__shfl_down_sync(kFull, t[c].x, o), __shfl_down_sync(kFull, t[c].y, o)));
-    if (lane == 0) {
-        sh[2 * warp] = make_float4(t[0].x, t[0].y, t[1].x, t[1].y);
-        sh[2 * warp + 1] = make_float4(t[2].x, t[2].y, t[3].x, t[3].y);
-    }
-    __syncthreads();
-    if (warp == 0) {
-        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 w0 = lane < NT / 32 ? sh[2 * lane] : z, w1 = lane < NT / 32 ? sh[2 * lane + 1] : z;
-        t[0] = make_float2(w0.x, w0.y); t[1] = make_float2(w0.z, w0.w);
-        t[2] = make_float2(w1.x, w1.y); t[3] = make_float2(w1.z, w1.w);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                t[c] = df_add(t[c], make_float2(__shfl_down_sync(kFull, t[c].x, o), __shfl_down_sync(kFull, t[c].y, o)));
-        if (lane == 0)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) out[c] = df_to(t[c]);
-    }
 }
 
 // Returns true in every thread of the block that is the last of its scene to finish.  Callers
@@ -1422,32 +1347,25 @@ __global__ void __launch_bounds__(BS) k_cg_update(Dev d, Params p, unsigned long
 }
 
 // ---- three-pass form (the reference's CGSolver arrangement, MPSSolver.cuh:33-60)
-// Pass 1 (k_cg_ap3): A p and the block sums of r.r, p.Ap, r.Ap and Ap.Ap.  Pass 2
-// (k_cg_decide3): the stop test r.r < tol, alpha = r.r / p.Ap, and beta = (r.r)_new / r.r with
-// (r.r)_new = (r - alpha Ap).(r - alpha Ap) = r.r - 2 alpha r.Ap + alpha^2 Ap.Ap, so that pass 3
-// (k_cg_vec3) updates x, r and p in one sweep.  The reference forms (r.r)_new from the updated r
-// after a separate residual pass; the two agree to the rounding of the FP32 residuals (about 1e-7
-// of beta), and the stop test still reads r.r of the stored residual, in the next pass 1.
+// A p, dots r.r and p.Ap, the stop test and alpha = r.r / p.Ap.
 
-// The end of pass 1 for slot i (live: a fluid slot of the scene): stores Ap and the block's
-// partial sums.
+// The end of the operator pass for slot i (live: a fluid slot of the scene): stores Ap and the
+// block's partial sums of r.r and p.Ap.
 template <int BS>
-__device__ __forceinline__ void ap3_finish(const Dev& d, int i, bool live, float4 q, float3 a, float4* sh) {
-    float rr = 0.0f, pap = 0.0f, rap = 0.0f, apap = 0.0f;
+__device__ __forceinline__ void ap3_finish(const Dev& d, int i, bool live, float4 q, float3 a, float2* sh) {
+    float rr = 0.0f, pap = 0.0f;
     if (live) {
         d.cg_ap[i] = make_float4(a.x, a.y, a.z, 0.0f);
         const float4 r = d.cg_r[i];
         rr = r.x * r.x + r.y * r.y + r.z * r.z;
         pap = q.x * a.x + q.y * a.y + q.z * a.z;
-        rap = r.x * a.x + r.y * a.y + r.z * a.z;
-        apap = a.x * a.x + a.y * a.y + a.z * a.z;
     }
-    block_partial4<BS>(d, rr, pap, rap, apap, sh);
+    block_partial2<BS>(d, rr, pap, sh);
 }
 
 template <int BS>
 __global__ void MPSG_BOUNDS_AP(BS) k_cg_ap3(Dev d, Params p, unsigned long long cond, int use_cond) {
-    __shared__ float4 sh4[BS / 32];
+    __shared__ float2 sh2[BS / 32];
     const int i = blockIdx.x * BS + threadIdx.x;
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
@@ -1463,7 +1381,7 @@ __global__ void MPSG_BOUNDS_AP(BS) k_cg_ap3(Dev d, Params p, unsigned long long 
         const unsigned c = d.cnt[i];
         a = apply_A(d, p, i, d.cg_p, p.cg_factor, xi, q, c);
     }
-    ap3_finish<BS>(d, i, live, q, a, sh4);
+    ap3_finish<BS>(d, i, live, q, a, sh2);
 }
 
 // k_cg_ap3 with the neighbours' positions and directions gathered from the block's tile
@@ -1472,7 +1390,7 @@ template <int BS>
 __global__ void __launch_bounds__(BS) k_cg_ap3_tile(Dev d, Params p, unsigned long long cond, int use_cond) {
     constexpr int TM = kTilePerSlot * BS;
     extern __shared__ float4 tile[];   // TM positions, then TM directions
-    __shared__ float4 sh4[BS / 32];
+    __shared__ float2 sh2[BS / 32];
     const int i = blockIdx.x * BS + threadIdx.x;
     const int s = block_scene(d, BS);
     if (use_cond != 2 && !d.solve[s].active) return;   // use_cond 2: profiling form (no decision follows)
@@ -1502,15 +1420,15 @@ __global__ void __launch_bounds__(BS) k_cg_ap3_tile(Dev d, Params p, unsigned lo
         a = tiled ? apply_A_tile(d, p, i, tile, tile + TM, T, p.cg_factor, xi, q, c)
                   : apply_A(d, p, i, d.cg_p, p.cg_factor, xi, q, c);
     }
-    ap3_finish<BS>(d, i, live, q, a, sh4);
+    ap3_finish<BS>(d, i, live, q, a, sh2);
 }
 
-// The three-pass CG's decision after k_cg_ap3 (one 1024-thread block per scene): r.r, p.Ap, r.Ap
-// and Ap.Ap from the operator pass's per-block partials, the stop test r.r < tol, alpha = r.r /
-// p.Ap, beta, the loop counter (MPSSolver.cuh:33-60).
+// The three-pass CG's decision after k_cg_ap3 (one 1024-thread block per scene): r.r and p.Ap
+// from the operator pass's per-block partials, the stop test r.r < tol, alpha = r.r / p.Ap, the
+// loop counter (MPSSolver.cuh:33-60).
 __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, int bs, unsigned long long cond,
                                                                int use_cond) {
-    __shared__ float4 sh[2 * (kDecideThreads / 32)];
+    __shared__ double2 sh[32];
     pdl_release();
     const int s = blockIdx.x;
     SceneSolve& S = d.solve[s];
@@ -1519,10 +1437,9 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, 
         return;
     }
     const Scene& sc = d.scenes[s];
-    double t[4];
-    scene_partials4<kDecideThreads>(d, sc, bs, sh, t);
+    const double2 t = scene_partials<kDecideThreads, 2>(d, sc, bs, sh);
     if (threadIdx.x == 0) {
-        const double trr = t[0], tpap = t[1], trap = t[2], tapap = t[3];
+        const double trr = t.x, tpap = t.y;
         const int l = S.iter;
         const int cap = p.fixed_iters > 0 ? p.fixed_iters : p.cg_max_iter;
         const bool stop = p.fixed_iters > 0 ? false : (trr < p.cg_tol_d);
@@ -1533,9 +1450,7 @@ __global__ void __launch_bounds__(kDecideThreads) k_cg_decide3(Dev d, Params p, 
             S.do_update = 0;
         } else {
             S.do_update = 1;
-            const double al = trr / tpap;
-            S.cg_alpha = al;
-            S.cg_beta = (trr - 2.0 * al * trap + al * al * tapap) / trr;
+            S.cg_alpha = trr / tpap;
             S.iter = l + 1;
             if (l + 1 > cap) S.active = 0;
         }
@@ -1556,25 +1471,66 @@ constexpr int kVecSlots = 256;
 #endif
 
 
-// Pass 3: x += alpha p, r -= alpha Ap, p = r + beta p (MPSSolver.cuh:49-60, MPSCGKernel.cuh:196-207)
-// with alpha and beta from k_cg_decide3; the loop guard of the WHILE body.
+// r -= alpha Ap, beta = (r.r)_new / (r.r)_old.  (x += alpha p is left to k_cg_dir3, which reads p
+// anyway: the same arithmetic, 16 fewer bytes a slot per iteration.)
 template <int NT>
-__global__ void __launch_bounds__(NT) k_cg_vec3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+__global__ void __launch_bounds__(NT) k_cg_update3(Dev d, Params p, int profile) {
     constexpr int U = kVecSlots / NT;
-    if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
-    // the grid covers exactly the allocated slots, so the vectors load before the wait for the
-    // decision and the scene and solver-state lookups (padding slots are loaded and not used)
+    // the grid covers exactly the allocated slots, so the data loads go out before the scene and
+    // solver-state lookups (padding slots are loaded and not used)
     const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
-    float4 x[U], r[U], q[U], w[U];
+    float4 r[U], ap[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int i = i0 + u * NT;
-        x[u] = d.cg_x[i];
         r[u] = d.cg_r[i];
-        q[u] = d.cg_p[i];
-        w[u] = d.cg_ap[i];
+        ap[u] = d.cg_ap[i];
     }
-    pdl_wait();   // alpha, beta and do_update come from k_cg_decide3
+    pdl_wait();   // alpha and do_update come from k_cg_decide3
+    const int s = block_scene(d, kVecSlots);
+    if (!profile && !d.solve[s].do_update) return;
+    const Scene& sc = d.scenes[s];
+    const int end = sc.slot_begin + sc.n;
+    const float a = float(d.solve[s].cg_alpha);
+    float rr = 0.0f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * NT;
+        if (i < end) {
+            r[u].x -= a * ap[u].x; r[u].y -= a * ap[u].y; r[u].z -= a * ap[u].z;
+            d.cg_r[i] = r[u];
+            rr += r[u].x * r[u].x + r[u].y * r[u].y + r[u].z * r[u].z;
+        }
+    }
+    warp_acc_put<1>(d, p, s, profile != 0, rr, 0.0f);
+}
+
+// beta = (r.r)_new / (r.r)_old from k_cg_update3's sums (the scene's accumulator), one warp per
+// scene that is updating.
+__global__ void __launch_bounds__(kAccDecideThreads) k_cg_beta3(Dev d) {
+    pdl_release();
+    const int s = blockIdx.x;
+    SceneSolve& S = d.solve[s];
+    if (!S.do_update) return;
+    const double t = acc_take(d, s, 0);
+    if (threadIdx.x == 0) S.cg_beta = t / S.rr;
+}
+
+// x += alpha p with the old direction, then p = r + beta p (MPSCGKernel.cuh:196-207); the loop
+// guard of the WHILE body.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_cg_dir3(Dev d, Params p, unsigned long long cond, int use_cond, int limit) {
+    constexpr int U = kVecSlots / NT;
+    if (use_cond == 1 && blockIdx.x == 0 && threadIdx.x == 0) loop_guard(d, cond, limit);
+    const int i0 = blockIdx.x * kVecSlots + threadIdx.x;
+    float4 x[U], r[U], q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {   // loads before the lookups, as in k_cg_update3
+        x[u] = d.cg_x[i0 + u * NT];
+        r[u] = d.cg_r[i0 + u * NT];
+        q[u] = d.cg_p[i0 + u * NT];
+    }
+    pdl_wait();   // beta comes from k_cg_beta3
     const int s = block_scene(d, kVecSlots);
     if (use_cond != 2 && !d.solve[s].do_update) return;   // use_cond 2: profiling form
     const Scene& sc = d.scenes[s];
@@ -1586,10 +1542,8 @@ __global__ void __launch_bounds__(NT) k_cg_vec3(Dev d, Params p, unsigned long l
         const int i = i0 + u * NT;
         if (i < end) {
             x[u].x += a * q[u].x; x[u].y += a * q[u].y; x[u].z += a * q[u].z;
-            r[u].x -= a * w[u].x; r[u].y -= a * w[u].y; r[u].z -= a * w[u].z;
-            q[u].x = r[u].x + b * q[u].x; q[u].y = r[u].y + b * q[u].y; q[u].z = r[u].z + b * q[u].z;
             d.cg_x[i] = x[u];
-            d.cg_r[i] = r[u];
+            q[u].x = r[u].x + b * q[u].x; q[u].y = r[u].y + b * q[u].y; q[u].z = r[u].z + b * q[u].z;
             d.cg_p[i] = q[u];
         }
     }
@@ -1868,16 +1822,26 @@ void launch_cg_ap3(const Dev& d, const Params& p, int bs, unsigned long long con
     }
     if (use_cond != 2) k_cg_decide3<<<p.nscenes, kDecideThreads, 0, s>>>(d, p, bs, cond, use_cond);
 }
-void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
-    k_cg_vec3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0ull, 2, 0);
+void launch_cg_update3(const Dev& d, const Params& p, int bs, cudaStream_t s) {
+    (void)bs;
+#if MPSG_VEC_PDL
+    launch_after_decide(k_cg_update3<MPSG_VEC_NT>, p.slots / kVecSlots, MPSG_VEC_NT, s, d, p, 0);
+#else
+    k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0);
+#endif
+    k_cg_beta3<<<p.nscenes, kAccDecideThreads, 0, s>>>(d);
 }
-void launch_cg_vec3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
+void launch_cg_vector_profile(const Dev& d, const Params& p, cudaStream_t s) {
+    k_cg_update3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 1);
+    k_cg_dir3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, 0ull, 2, 0);
+}
+void launch_cg_dir3(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,
                     cudaStream_t s) {
     (void)bs;
 #if MPSG_VEC_PDL
-    launch_after_decide(k_cg_vec3<MPSG_VEC_NT>, p.slots / kVecSlots, MPSG_VEC_NT, s, d, p, cond, use_cond, limit);
+    launch_after_decide(k_cg_dir3<MPSG_VEC_NT>, p.slots / kVecSlots, MPSG_VEC_NT, s, d, p, cond, use_cond, limit);
 #else
-    k_cg_vec3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, cond, use_cond, limit);
+    k_cg_dir3<MPSG_VEC_NT><<<p.slots / kVecSlots, MPSG_VEC_NT, 0, s>>>(d, p, cond, use_cond, limit);
 #endif
 }
 void launch_jacobi(const Dev& d, const Params& p, int bs, unsigned long long cond, int use_cond, int limit,

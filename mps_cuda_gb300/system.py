@@ -217,8 +217,8 @@ class Simulation:
         if self.cfg.stage == 1:
             static += 1   # the neighbourhood tiles, built with the neighbour lists
         # per pass: pressure A + its decision + pressure B; three-pass CG: operator + decision +
-        # vector pass; two-pass: operator + decision + update; Jacobi: one sweep
-        cg = 1 if jacobi else 3
+        # update + beta + direction; two-pass: operator + decision + update; Jacobi: one sweep
+        cg = 1 if jacobi else (3 if self.cfg.cg_form == L.CG_TWO_PASS else 5)
         return static + 3 * runs[0] + cg * runs[1] + 3 * runs[2]
 
 

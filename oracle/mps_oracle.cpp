@@ -715,6 +715,15 @@ orc_sim* orc_create(const orc_params* p) {
 
 void orc_destroy(orc_sim* s) { delete s; }
 
+// Replaces the parameters (tolerances, iteration caps, fixed_iters, ...) of a live replay; the
+// precision study reruns one solve with another iteration count from the same state.
+void orc_set_params(orc_sim* s, const orc_params* p) {
+    s->p = *p;
+#ifdef _OPENMP
+    if (p->threads > 0) omp_set_num_threads(p->threads);
+#endif
+}
+
 int orc_set_fluid(orc_sim* s, int64_t n, const double* pos, const double* vel, const double* mass,
                   const double* radius, const uint32_t* ids) {
     if (n < 0) return -1;

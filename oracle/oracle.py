@@ -58,6 +58,7 @@ def load() -> C.CDLL:
         lib.orc_create.restype = vp
         lib.orc_create.argtypes = [C.POINTER(Params)]
         lib.orc_destroy.argtypes = [vp]
+        lib.orc_set_params.argtypes = [vp, C.POINTER(Params)]
         lib.orc_set_fluid.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp]
         lib.orc_set_boundary.argtypes = [vp, C.c_int64, vp, vp, vp]
         lib.orc_set_frame.argtypes = [vp, C.c_int32]
@@ -142,6 +143,11 @@ class Oracle:
         vol = None if volume is None else np.ascontiguousarray(volume, np.float64)
         self.nb = pos.shape[0]
         self.lib.orc_set_boundary(self.h, self.nb, _p(pos), _p(radius), None if vol is None else _p(vol))
+
+    def set_fixed_iters(self, n: int):
+        """fixed_iters of the following phases (0: adaptive loops)."""
+        self.p.fixed_iters = int(n)
+        self.lib.orc_set_params(self.h, C.byref(self.p))
 
     def set_frame(self, f: int):
         self.lib.orc_set_frame(self.h, f)
