@@ -66,6 +66,32 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 #else
 #define MPSG_BOUNDS_PB(BS) __launch_bounds__(BS)
 #endif
+// The same for the once-a-step passes: solve set-up (k_cg_b), density (k_density_alpha) and
+// neighbour build (k_build_nbrs).
+#ifndef MPSG_MINW_SETUP
+#define MPSG_MINW_SETUP 0
+#endif
+#ifndef MPSG_MINW_DENS
+#define MPSG_MINW_DENS 0
+#endif
+#ifndef MPSG_MINW_BUILD
+#define MPSG_MINW_BUILD 0
+#endif
+#if MPSG_MINW_SETUP > 0
+#define MPSG_BOUNDS_SETUP(BS) __launch_bounds__(BS, MPSG_MINW_SETUP / ((BS) / 32))
+#else
+#define MPSG_BOUNDS_SETUP(BS) __launch_bounds__(BS)
+#endif
+#if MPSG_MINW_DENS > 0
+#define MPSG_BOUNDS_DENS(BS) __launch_bounds__(BS, MPSG_MINW_DENS / ((BS) / 32))
+#else
+#define MPSG_BOUNDS_DENS(BS) __launch_bounds__(BS)
+#endif
+#if MPSG_MINW_BUILD > 0
+#define MPSG_BOUNDS_BUILD(BS) __launch_bounds__(BS, MPSG_MINW_BUILD / ((BS) / 32))
+#else
+#define MPSG_BOUNDS_BUILD(BS) __launch_bounds__(BS)
+#endif
 
 __device__ __forceinline__ int block_scene(const Dev& d, int bs) {
     return d.chunk_scene[(blockIdx.x * bs) / kChunk];
@@ -505,7 +531,7 @@ __constant__ unsigned char kKeyOrder[4][27] = {
 };
 
 template <int BS>
-__global__ void __launch_bounds__(BS) k_build_nbrs(Dev d, Params p) {
+__global__ void MPSG_BOUNDS_BUILD(BS) k_build_nbrs(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
     const Scene& sc = d.scenes[block_scene(d, BS)];
     __shared__ unsigned long long s_pf, s_pb;
@@ -634,7 +660,7 @@ __global__ void k_bvolume(Dev d, Params p, int nb, int accumulate) {
 // results are the same bits.  `parts` selects the neighbour sets of the sums (1 fluid, 2 boundary).
 constexpr int W_DENSITY = 1, W_COLOR = 2, W_ALPHA = 4, W_GRAVITY = 8, W_ALL = 15;
 template <int BS, int WHAT>
-__global__ void __launch_bounds__(BS) k_density_alpha(Dev d, Params p, int parts) {
+__global__ void MPSG_BOUNDS_DENS(BS) k_density_alpha(Dev d, Params p, int parts) {
     const int i = blockIdx.x * BS + threadIdx.x;
     const Scene& sc = d.scenes[block_scene(d, BS)];
     if (i >= sc.slot_begin + sc.n) return;
@@ -986,7 +1012,7 @@ __global__ void __launch_bounds__(BS) k_st_factor(Dev d, Params p) {
 //   cv_ij = 10 rho0 mu / rho_i * (m_i + m_j) / 2 / rho_j / (d^2 + 0.01 h_i^2) * G_ij / (d + eps)
 //                                                                           (viscosity, :628-633)
 template <int BS>
-__global__ void __launch_bounds__(BS) k_cg_b(Dev d, Params p) {
+__global__ void MPSG_BOUNDS_SETUP(BS) k_cg_b(Dev d, Params p) {
     const int i = blockIdx.x * BS + threadIdx.x;
     const Scene& sc = d.scenes[block_scene(d, BS)];
     if (i >= sc.slot_begin + sc.n) return;
