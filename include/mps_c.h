@@ -76,7 +76,8 @@ typedef struct mps_config {
     int32_t cg_max_iter;
     double cg_factor;
     int32_t fixed_iters;         /* > 0: DF, CD and CG each run exactly this many iterations */
-    int32_t max_fluid_neighbors; /* list capacity per particle (overflow -> MPS_E_OVERFLOW) */
+    int32_t max_fluid_neighbors; /* list capacity per particle (overflow -> MPS_E_OVERFLOW); 0 = 96,
+                                    above 65535 (16-bit counts) mps_create returns MPS_E_INVALID */
     int32_t max_boundary_neighbors;
     int32_t volume_accumulate;   /* 1: reproduce the un-reset boundary volume (MPSSystem.cpp:237-238) */
     int32_t use_graph;           /* 1: whole step as one CUDA graph with device-side loops */

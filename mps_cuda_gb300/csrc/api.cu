@@ -785,6 +785,8 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     if (!mat || !phys || !out) return fail(MPS_E_INVALID, "null argument");
     if (!(phys->dt > 0.0)) return fail(MPS_E_INVALID, "dt must be positive");
     if (!(mat->density > 0.0) || !(mat->volume > 0.0)) return fail(MPS_E_INVALID, "density and volume must be positive");
+    if (cfg && (cfg->max_fluid_neighbors > 65535 || cfg->max_boundary_neighbors > 65535))
+        return fail(MPS_E_INVALID, "neighbour capacity above 65535 (the per-slot counts are 16-bit)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -796,8 +798,8 @@ static int create_common(const mps_material* mat, const mps_physics* phys, const
     h->mat = *mat;
     h->phys = *phys;
     if (cfg) h->cfg = *cfg; else mps_default_config(&h->cfg);
-    if (h->cfg.max_fluid_neighbors <= 0 || h->cfg.max_fluid_neighbors > 65535) h->cfg.max_fluid_neighbors = 96;
-    if (h->cfg.max_boundary_neighbors <= 0 || h->cfg.max_boundary_neighbors > 65535) h->cfg.max_boundary_neighbors = 64;
+    if (h->cfg.max_fluid_neighbors <= 0) h->cfg.max_fluid_neighbors = 96;
+    if (h->cfg.max_boundary_neighbors <= 0) h->cfg.max_boundary_neighbors = 64;
     if (h->cfg.max_iter <= 0) h->cfg.max_iter = 100;
     if (h->cfg.cg_max_iter <= 0) h->cfg.cg_max_iter = 100;
     if (h->cfg.sort_digit_bits < 1 || h->cfg.sort_digit_bits > 8) h->cfg.sort_digit_bits = 8;

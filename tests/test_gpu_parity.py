@@ -369,6 +369,21 @@ def test_single_particle_and_single_pair(mps, orc):
         assert rel_err(v[:, :3], o.get("vel")) < REL, keep
 
 
+def test_empty_fluid_and_limits(mps):
+    """A single-scene handle without fluid is rejected (a batch accepts empty scenes, below), and so
+    is a box whose cell grid would exceed the key space; both with MPS_E_INVALID."""
+    from mps_cuda_gb300 import MpsError, Simulation
+    base = scenes_mod().dam_break_small(4, seed=3)
+    empty = dataclasses.replace(base, pos4=base.pos4[:0].copy(), vel4=base.vel4[:0].copy(), name="empty")
+    with pytest.raises(MpsError, match="INVALID"):
+        Simulation.from_scene(empty)
+    huge = dataclasses.replace(base, physics=dict(base.physics, max=(1.0e7, 1.0e7, 1.0e7)), name="huge")
+    with pytest.raises(MpsError, match="INVALID"):
+        Simulation.from_scene(huge)
+    with pytest.raises(MpsError, match="INVALID"):
+        Simulation.from_scene(base, max_fluid_neighbors=70000)
+
+
 def test_batched_with_an_empty_scene(mps):
     """A scene without fluid particles in the middle of a batch: the other scenes step exactly as
     they do alone."""

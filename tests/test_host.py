@@ -62,6 +62,9 @@ def test_invalid_arguments_rejected_without_device(mps):
         lib.mps_destroy(h)
     assert lib.mps_step(None, 1, None) == -1
     assert lib.mps_get_stats(None, None, None) == -1
+    cfg = mps._lib.default_config(max_fluid_neighbors=70000)   # above the 16-bit counts
+    assert lib.mps_create(C.byref(mat), C.byref(phys), C.byref(cfg), 0, C.byref(h)) == -1
+    assert b"65535" in lib.mps_last_error()
 
 
 def _digest(*arrays):
