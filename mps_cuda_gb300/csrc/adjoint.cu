@@ -71,8 +71,10 @@ struct AdjointStore {
     float4 *qbar0 = nullptr, *qbar1 = nullptr, *bbar = nullptr, *gg = nullptr;
     float4 *Dbar = nullptr, *Dbar2 = nullptr;   // symmetric 3x3 cotangent of the Jacobi block: (xx, yy, zz, xy), (xz, yz)
     float4 *y0 = nullptr, *y1 = nullptr;        // D^-1 qbar of a reverse sweep's input / output
-    float *grho = nullptr, *galpha = nullptr, *gdelta = nullptr, *gsf = nullptr;
+    float *grho = nullptr, *galpha = nullptr, *gsf = nullptr;
     double *gsig = nullptr, *gmu = nullptr;   // per-slot parameter cotangents (FP64)
+    float4* pa = nullptr;            // per slot (dt gv where the mass is positive, kappa): pass A's neighbour data
+    float4* pb = nullptr;            // per slot (u, delta cotangent): pass B's neighbour data
     float2* pc = nullptr;            // per pair (cbar, cvbar), interleaved like nbr_f
     float4* px = nullptr;            // per pair explicit x_ij cotangent
     unsigned char* rev = nullptr;    // per pair: position of i in the neighbour's list
@@ -84,7 +86,8 @@ struct AdjointStore {
         void* ptrs[] = {cp_pos, cp_vel, cp_ids, fin_pos, fin_vel, fin_ids, t_udf, t_ucd, t_q, t_x, t_kdf, t_kcd,
                         t_cdf, t_ccd, t_adv, t_nbrf, t_nbrb, t_cnt, t_ids, t_coef, t_aux, t_jd, t_jd2, t_rho,
                         t_alpha, gx, gv, gx_id, gv_id, qbar0, qbar1, bbar,
-                        Dbar, Dbar2, y0, y1, gg, grho, galpha, gdelta, gsf, gsig, gmu, pc, px, rev, gparam, flag, ctr_save};
+                        Dbar, Dbar2, y0, y1, gg, grho, galpha, gsf, gsig, gmu, pa, pb, pc, px, rev, gparam, flag,
+                        ctr_save};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         *this = AdjointStore{};
@@ -190,7 +193,7 @@ __device__ __forceinline__ void visit2(const unsigned* __restrict__ list, size_t
     }
 }
 constexpr int kAdjBatch = 2;
-struct AG { float4 x, g; float k, m; };          // pass A: position, velocity cotangent, stiffness, mass
+struct AG { float4 x, a; };                      // pass A: position, (dt gv masked by the mass, stiffness)
 struct BG { float4 x, u; };                      // pass B: position, velocity (w: delta cotangent)
 struct JS { float2 c; unsigned rv; };            // Jacobi reverse, streamed: own coefficient, reverse index
 struct JG { float4 x, y, q; float2 cji; };
@@ -272,9 +275,21 @@ __global__ void k_adj_advect(Dev d, Params p, const unsigned char* code, float4*
 // First half of one DF/CD iteration's reverse: abar = dt ubar' (massive particles), the
 // stiffness cotangent kbar_i, its chain through the clamp / min branch into delta, rho, alpha,
 // and the x cotangent of the pressure-force terms.
+// What the reverse of pass A gathers from each neighbour, in one 16-byte record: dt gv (zero for a
+// particle without mass, which pass B leaves unchanged) and the iteration's stiffness.
+__global__ void __launch_bounds__(kAB) k_adj_pack_a(Dev d, Params p, const float4* gv, const float* kap, float4* pa) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.slots) return;
+    int s;
+    if (!slot_live(d, i, s)) return;
+    const float4 g = gv[i];
+    const bool m = d.vel[i].w > 1.0e-10f;
+    pa[i] = make_float4(m ? p.dt * g.x : 0.0f, m ? p.dt * g.y : 0.0f, m ? p.dt * g.z : 0.0f, kap[i]);
+}
+
 __global__ void __launch_bounds__(kAB) k_adj_pA(Dev d, Params p, const float4* X, const float* kap,
-                                                 const unsigned char* code, const float4* gv, float* gdelta,
-                                                 float* grho, float* galpha, float4* gx) {
+                                                 const unsigned char* code, const float4* gv, const float4* pa,
+                                                 const float4* U, float4* pb, float* grho, float* galpha, float4* gx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.slots) return;
     int s;
@@ -291,11 +306,11 @@ __global__ void __launch_bounds__(kAB) k_adj_pA(Dev d, Params p, const float4* X
     float kbar = 0.0f;
     float3 xa = make_float3(0.f, 0.f, 0.f);
     visit2<kAdjBatch, NoStream, AG>(d.nbr_f, S, i, nf, [&](int) { return NoStream{}; },
-                                    [&](unsigned j, NoStream, int) { return AG{X[j], gv[j], kap[j], d.vel[j].w}; },
+                                    [&](unsigned j, NoStream, int) { return AG{X[j], pa[j]}; },
                                     [&](const AG& t, NoStream, int) {
         const float4 xj = t.x;
-        const float kj = t.k;
-        const float3 aj = t.m > 1.0e-10f ? p.dt * f3(t.g) : make_float3(0.f, 0.f, 0.f);
+        const float kj = t.a.w;
+        const float3 aj = f3(t.a);
         const float3 e = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
         const float r = sqrtf(dot3(e, e));
         const KD Ki = kern_d(r, invhi, p.cubic);
@@ -331,12 +346,13 @@ __global__ void __launch_bounds__(kAB) k_adj_pA(Dev d, Params p, const float4* X
         gd = kb * p.dt;
         if (cd == 2) grho[i] += kb * p.inv_rho0;
     }
-    gdelta[i] = gd;
+    const float4 u = U[i];
+    pb[i] = make_float4(u.x, u.y, u.z, gd);   // pass B's reverse gathers velocity and delta cotangent together
 }
 
 // Second half: the delta terms' cotangents into u^k and x.
-__global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X, const float4* U,
-                                                 const float* gdelta, float4* gv, float4* gx) {
+__global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X, const float4* pb, float4* gv,
+                                                 float4* gx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.slots) return;
     int s;
@@ -344,13 +360,14 @@ __global__ void __launch_bounds__(kAB) k_adj_pB(Dev d, Params p, const float4* X
     const size_t S = size_t(p.slots);
     const float4 xi = X[i];
     const float invhi = 1.0f / xi.w;
-    const float3 ui = f3(U[i]);
-    const float di = gdelta[i];
+    const float4 ub = pb[i];
+    const float3 ui = f3(ub);
+    const float di = ub.w;
     const unsigned c = d.cnt[i];
     const int nf = int(c & 0xffffu), nb = int(c >> 16);
     float3 au = make_float3(0.f, 0.f, 0.f), xa = make_float3(0.f, 0.f, 0.f);
     visit2<kAdjBatch, NoStream, BG>(d.nbr_f, S, i, nf, [&](int) { return NoStream{}; },
-                                    [&](unsigned j, NoStream, int) { float4 u = U[j]; u.w = gdelta[j]; return BG{X[j], u}; },
+                                    [&](unsigned j, NoStream, int) { return BG{X[j], pb[j]}; },
                                     [&](const BG& t, NoStream, int) {
         const float4 xj = t.x;
         const float dj = t.u.w;
@@ -818,7 +835,7 @@ size_t store_bytes(const mps_handle* h, int nsteps, int every) {
     step += (cap + capb + 2) * S * sizeof(unsigned) + cap * S * sizeof(float2);   // lists, counts, ids, coefficients
     step += S * (sizeof(float2) + 2 * sizeof(float4) + 2 * sizeof(float));      // aux, Jacobi blocks, rho, alpha
     b += E * step;
-    b += 12 * S * sizeof(float4) + 4 * S * sizeof(float) + 2 * S * sizeof(double);   // cotangents
+    b += 14 * S * sizeof(float4) + 3 * S * sizeof(float) + 2 * S * sizeof(double);   // cotangents
     b += cap * S * (sizeof(float2) + sizeof(float4) + 1);   // per-pair cotangents + reverse index
     b += size_t(h->nscenes) * 2 * sizeof(double) + 64;
     return b;
@@ -874,11 +891,11 @@ int ensure_store(mps_handle* h, int nsteps, int every) {
     ADJ_TRY(alloc(&A.t_jd2, E * S, t));
     ADJ_TRY(alloc(&A.t_rho, E * S, t));
     ADJ_TRY(alloc(&A.t_alpha, E * S, t));
-    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.Dbar2, &A.gg, &A.y0, &A.y1};
+    float4** f4[] = {&A.gx, &A.gv, &A.qbar0, &A.qbar1, &A.bbar, &A.Dbar, &A.Dbar2, &A.gg, &A.y0, &A.y1, &A.pa, &A.pb};
     for (float4** q : f4) ADJ_TRY(alloc(q, S, t));
     ADJ_TRY(alloc(&A.gx_id, size_t(std::max<int64_t>(h->n, 1)), t));
     ADJ_TRY(alloc(&A.gv_id, size_t(std::max<int64_t>(h->n, 1)), t));
-    float** f1[] = {&A.grho, &A.galpha, &A.gdelta, &A.gsf};
+    float** f1[] = {&A.grho, &A.galpha, &A.gsf};
     for (float** q : f1) ADJ_TRY(alloc(q, S, t));
     ADJ_TRY(alloc(&A.gsig, S, t));
     ADJ_TRY(alloc(&A.gmu, S, t));
@@ -1046,9 +1063,10 @@ int adjoint_step(mps_handle* h, const Slot& t, cudaStream_t s) {
     k_adj_advect<<<nb, kAB, 0, s>>>(d, p, t.adv, A.gx, A.gv);
     // constant-density solve
     for (int k = K - 1; k >= 0; --k) {
-        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, t.x, t.kcd + size_t(k) * S, t.ccd + size_t(k) * S, A.gv, A.gdelta,
-                                     A.grho, A.galpha, A.gx);
-        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, t.x, t.ucd + size_t(k) * S, A.gdelta, A.gv, A.gx);
+        k_adj_pack_a<<<nb, kAB, 0, s>>>(d, p, A.gv, t.kcd + size_t(k) * S, A.pa);
+        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, t.x, t.kcd + size_t(k) * S, t.ccd + size_t(k) * S, A.gv, A.pa,
+                                     t.ucd + size_t(k) * S, A.pb, A.grho, A.galpha, A.gx);
+        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, t.x, A.pb, A.gv, A.gx);
     }
     // viscosity + surface tension (Jacobi)
     ADJ_TRY(cudaMemsetAsync(A.pc, 0, cap * S * sizeof(float2), s));
@@ -1074,9 +1092,10 @@ int adjoint_step(mps_handle* h, const Slot& t, cudaStream_t s) {
     k_adj_stfac<<<nb, kAB, 0, s>>>(d, p, t.x, V0, A.gsf, A.gv, A.gx);
     // divergence-free solve
     for (int k = K - 1; k >= 0; --k) {
-        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, t.x, t.kdf + size_t(k) * S, t.cdf + size_t(k) * S, A.gv, A.gdelta,
-                                     A.grho, A.galpha, A.gx);
-        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, t.x, t.udf + size_t(k) * S, A.gdelta, A.gv, A.gx);
+        k_adj_pack_a<<<nb, kAB, 0, s>>>(d, p, A.gv, t.kdf + size_t(k) * S, A.pa);
+        k_adj_pA<<<nb, kAB, 0, s>>>(d, p, t.x, t.kdf + size_t(k) * S, t.cdf + size_t(k) * S, A.gv, A.pa,
+                                     t.udf + size_t(k) * S, A.pb, A.grho, A.galpha, A.gx);
+        k_adj_pB<<<nb, kAB, 0, s>>>(d, p, t.x, A.pb, A.gv, A.gx);
     }
     // gravity is the identity; density and alpha
     k_adj_dens_a<<<nb, kAB, 0, s>>>(d, p, t.x, A.galpha, A.gg);
