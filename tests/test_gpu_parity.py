@@ -5,7 +5,7 @@ Tolerances (FP32 bulk vs FP64 oracle, same inputs):
     against the oracle's restatement of the same FP32 scheme; neighbour counts against the
     reference's FP64 test differ only for pairs within 1e-6 h of the support radius.
   - densities, alphas, pressure factors, velocities after a phase, from an identical state:
-    max|a - b| / max|b| <= 1e-5 (the north-star bound "1e-5 relative of an FP64 oracle").
+    max|a - b| / max|b| <= 1e-5 (the per-step bound: 1e-5 relative to an FP64 oracle).
     "Identical state": the GPU's FP32 state is what both sides start from (the oracle takes it
     exactly, FP32 values being FP64 values), before the step and before each solver phase.  The
     pressure factor from an identical state is the stiffness of a solve's first iteration
