@@ -1149,6 +1149,9 @@ int mps_profile_kernel(mps_handle* h, int32_t kernel, int32_t reps, void* stream
                 radix_sort_pairs(h->keys, h->vals, h->keys_tmp, h->vals_tmp, h->sort_counts, int(h->n), h->key_bits, h->cfg.sort_digit_bits, s);
                 launch_reorder(ds, p, int(h->n), s);
                 h->cur = 1 - h->cur;
+                // the lists (and the stage-1 tiles built from them) now name the old order: the
+                // tiles fall back to global gathers until the next neighbour build
+                if (h->tile_n) cudaMemsetAsync(h->tile_n, 0xff, (size_t(h->slots) / 64 + 1) * sizeof(int), s);
                 break;
             }
             default: break;
